@@ -1,0 +1,207 @@
+/*
+ * tdycore_gb300.h -- C-ABI drop-in for TDycore's MPFA-O Richards residual and
+ * Jacobian path, evaluated on one GB300 (sm_103a).
+ *
+ * Every entry point returns a TDyErrorCode (0 = success), mirroring the
+ * PetscErrorCode convention of the reference (include/tdycore.h:137-256).
+ * The last error message of the calling thread is available through
+ * TDyGetErrorMessage().
+ *
+ * Arrays are plain pointers with sizes; no PETSc, MPI or torch types appear.
+ * Host-pointer entry points copy to and from the device inside the call;
+ * the "...Device" variants take device pointers and a cudaStream_t (passed as
+ * void*; NULL means the handle's own stream) and return after enqueueing work.
+ *
+ * Each declaration cites the reference interface it replaces (file:line in
+ * the TDycore source tree).
+ */
+#ifndef TDYCORE_GB300_H
+#define TDYCORE_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int TDyErrorCode;
+typedef struct _p_TDy *TDy;
+
+/* Error codes: numeric values follow PETSc's (petscerror.h) so callers that
+ * test PETSC_ERR_* constants keep working. */
+#define TDY_SUCCESS              0
+#define TDY_ERR_MEM             55
+#define TDY_ERR_SUP             56
+#define TDY_ERR_ARG_WRONG       62
+#define TDY_ERR_ARG_OUTOFRANGE  63
+#define TDY_ERR_LIB             76
+#define TDY_ERR_USER            83
+#define TDY_ERR_ARG_NULL        85
+#define TDY_ERR_NOT_CONVERGED   91
+#define TDY_ERR_GPU             97
+
+/* Enumerations: identical names and values to include/tdycore.h:8-99 and
+ * include/tdycore.h:63-72 (MPFA-O options). */
+typedef enum { RICHARDS = 0, TH, SALINITY } TDyMode;
+typedef enum { MPFA_O = 0, MPFA_O_DAE, MPFA_O_TRANSIENTVAR, BDM, WY, FV_TPF } TDyDiscretization;
+typedef enum { MPFAO_GMATRIX_DEFAULT = 0, MPFAO_GMATRIX_TPF } TDyMPFAOGmatrixMethod;
+typedef enum { DIRICHLET_BC = 0, NEUMANN_BC, SEEPAGE_BC } TDyBoundaryConditionType;
+typedef enum {
+  WATER_DENSITY_CONSTANT = 0,
+  WATER_DENSITY_EXPONENTIAL = 1,
+  WATER_DENSITY_BATZLE_AND_WANG = 2
+} TDyWaterDensityType;
+typedef enum { WATER_VISCOSITY_CONSTANT = 0, WATER_VISCOSITY_BATZLE_AND_WANG = 1 } TDyWaterViscosityType;
+/* Characteristic-curve families (include/private/tdycharacteristiccurvesimpl.h:7-38). */
+typedef enum { SAT_FUNC_GARDNER = 0, SAT_FUNC_VAN_GENUCHTEN = 1 } TDySaturationType;
+typedef enum { REL_PERM_FUNC_IRMAY = 0, REL_PERM_FUNC_MUALEM = 1 } TDyRelativePermeabilityType;
+
+/* Spatial callbacks: same shape as include/tdycore.h:74-99 with
+ * PetscInt = int and PetscReal = double (32-bit-index PETSc build). */
+typedef void (*TDyScalarSpatialFunction)(int n, double *x, double *f);
+typedef void (*TDyVectorSpatialFunction)(int n, double *x, double *f);
+typedef void (*TDyTensorSpatialFunction)(int n, double *x, double *f);
+typedef void (*TDyScalarSpatialIntegerFunction)(int n, double *x, int *f);
+
+/* ---------------------------------------------------------------------- */
+/* Process-level setup: replaces TDyInit/TDyFinalize (include/tdycore.h:126-130).
+ * argv is scanned for -tdy_* options read later by TDySetFromOptions. */
+TDyErrorCode TDyInit(int argc, char **argv);
+TDyErrorCode TDyInitNoArguments(void);
+TDyErrorCode TDyFinalize(void);
+/* Appends options given as one string ("-tdy_gravity 9.8 -tdy_water_density
+ * EXPONENTIAL"); stands in for PetscOptionsInsertString. */
+TDyErrorCode TDyOptionsInsertString(const char *options);
+TDyErrorCode TDyOptionsClear(void);
+const char *TDyGetErrorMessage(void);
+
+/* Lifecycle: include/tdycore.h:137-143 (TDyCreate ... TDyDestroy).
+ * comm is accepted for signature compatibility and must describe a single
+ * process (pass NULL). */
+TDyErrorCode TDyCreate(void *comm, TDy *tdy);
+TDyErrorCode TDySetMode(TDy tdy, TDyMode mode);
+TDyErrorCode TDySetDiscretization(TDy tdy, TDyDiscretization discretization);
+/* Alias used by demo/SPE10/steady.c:109. */
+TDyErrorCode TDySetDiscretizationMethod(TDy tdy, TDyDiscretization discretization);
+TDyErrorCode TDySetFromOptions(TDy tdy);
+TDyErrorCode TDySetup(TDy tdy);
+/* Host half of TDySetup only (mesh, materials, transmissibility, pattern):
+ * for consumers of the setup arrays; entry points that evaluate on the GPU
+ * then return TDY_ERR_GPU. */
+TDyErrorCode TDySetupHost(TDy tdy);
+TDyErrorCode TDyDestroy(TDy *tdy);
+
+/* Mesh construction: replaces TDySetDMConstructor + DMPlexCreateBoxMesh
+ * (include/tdycore.h:140; demo/transient/transient_mpfaof90.F90:47).
+ * TDySetBoxMesh builds nx*ny*nz hexahedra over [lower, upper] with cells
+ * numbered x fastest, then y, then z, as DMPlexCreateBoxMesh does.
+ * TDySetExtrudedMesh builds a z-extruded mesh from a surface mesh of nc2
+ * polygons with nvpc (3 or 4) counter-clockwise vertices each, over nv2
+ * surface vertices (xy[2*nv2]) and nlayers layers whose vertex elevations are
+ * z[(nlayers+1)*nv2] (level-major).  Cells are numbered layer*nc2 + c2. */
+TDyErrorCode TDySetBoxMesh(TDy tdy, int nx, int ny, int nz, const double lower[3], const double upper[3]);
+TDyErrorCode TDySetExtrudedMesh(TDy tdy, int nv2, const double *xy, int nc2, int nvpc, const int *cells2d,
+                                int nlayers, const double *z);
+
+/* Material properties: include/tdycore.h:150-171. */
+TDyErrorCode TDySetWaterDensityType(TDy tdy, TDyWaterDensityType type);
+TDyErrorCode TDySetWaterViscosityType(TDy tdy, TDyWaterViscosityType type);
+TDyErrorCode TDySetConstantPorosity(TDy tdy, double porosity);
+TDyErrorCode TDySetPorosityFunction(TDy tdy, TDyScalarSpatialFunction f);
+TDyErrorCode TDySetConstantIsotropicPermeability(TDy tdy, double k);
+TDyErrorCode TDySetIsotropicPermeabilityFunction(TDy tdy, TDyScalarSpatialFunction f);
+TDyErrorCode TDySetConstantDiagonalPermeability(TDy tdy, const double k[3]);
+TDyErrorCode TDySetDiagonalPermeabilityFunction(TDy tdy, TDyVectorSpatialFunction f);
+TDyErrorCode TDySetConstantTensorPermeability(TDy tdy, const double k[9]);
+TDyErrorCode TDySetTensorPermeabilityFunction(TDy tdy, TDyTensorSpatialFunction f);
+TDyErrorCode TDySetConstantResidualSaturation(TDy tdy, double sr);
+TDyErrorCode TDySetResidualSaturationFunction(TDy tdy, TDyScalarSpatialFunction f);
+/* Per-cell values (extension; the reference sets per-point parameters through
+ * SaturationSetType/RelativePermeabilitySetType,
+ * src/materials/tdycharacteristiccurves.c:72-113,271-316). cells may be NULL
+ * to mean 0..n-1. */
+TDyErrorCode TDySetPorosityValuesLocal(TDy tdy, int n, const int *cells, const double *phi);
+TDyErrorCode TDySetPermeabilityValuesLocal(TDy tdy, int n, const int *cells, const double *k9);
+TDyErrorCode TDySetResidualSaturationValuesLocal(TDy tdy, int n, const int *cells, const double *sr);
+TDyErrorCode TDySetCharacteristicCurveVanGenuchtenValuesLocal(TDy tdy, int n, const int *cells, const double *m,
+                                                               const double *alpha);
+TDyErrorCode TDySetCharacteristicCurveMualemValuesLocal(TDy tdy, int n, const int *cells, const double *m);
+/* Switch the saturation family to Gardner for the given cells (n, m, alpha per
+ * cell) or the relative permeability family to Irmay (m per cell);
+ * src/materials/tdycharacteristiccurves.c:641-667 and :451-460. */
+TDyErrorCode TDySetCharacteristicCurveGardnerValuesLocal(TDy tdy, int n, const int *cells, const double *gn,
+                                                          const double *gm, const double *alpha);
+TDyErrorCode TDySetCharacteristicCurveIrmayValuesLocal(TDy tdy, int n, const int *cells, const double *m);
+
+/* Boundary conditions and sources: include/tdycore.h:190-197 and
+ * src/fv/mpfao/tdympfao.c:408-426 (MPFA-O options). */
+TDyErrorCode TDySetBoundaryPressureFunction(TDy tdy, TDyScalarSpatialFunction f);
+/* The reference's MPFA-O applies one boundary type to every boundary face;
+ * when this per-face function is set (reference: tdycore.c:1350), faces take
+ * the returned TDyBoundaryConditionType instead (extension). */
+TDyErrorCode TDySetBoundaryPressureTypeFunction(TDy tdy, TDyScalarSpatialIntegerFunction f);
+TDyErrorCode TDyMPFAOSetGmatrixMethod(TDy tdy, TDyMPFAOGmatrixMethod method);
+TDyErrorCode TDyMPFAOSetBoundaryConditionType(TDy tdy, TDyBoundaryConditionType bctype);
+/* Mass source per cell in kg/s (SNES form) or kg/s/m^3 (TS form); the
+ * reference's source_sink array (src/fv/mpfao/tdympfao.c:364-384), which it
+ * never fills, so the default of zero keeps parity. */
+TDyErrorCode TDySetSourceSinkValuesLocal(TDy tdy, int n, const int *cells, const double *q);
+
+/* Queries. */
+TDyErrorCode TDyGetNumCells(TDy tdy, int *ncells);
+TDyErrorCode TDyGetNumBoundaryFaces(TDy tdy, int *nbnd);
+TDyErrorCode TDyGetCellCentroids(TDy tdy, double *xyz);
+TDyErrorCode TDyGetCellVolumes(TDy tdy, double *vol);
+/* Fixed CSR pattern of the Jacobian (cells sharing a vertex, sorted columns):
+ * replaces TDyCreateJacobian (src/tdycore.c:2187) and the DMCreateMatrix
+ * FVM++ adjacency (src/tdydiscretization.c:156-170). Pointers stay valid
+ * until TDyDestroy. */
+TDyErrorCode TDyGetJacobianPattern(TDy tdy, int *nrows, int *nnz, const int **rowptr, const int **colidx);
+/* Vector/matrix creation are no-ops kept for call-sequence compatibility
+ * (src/tdycore.c:2166, :2187). */
+TDyErrorCode TDyCreateVectors(TDy tdy);
+TDyErrorCode TDyCreateJacobian(TDy tdy);
+
+/* ---------------------------------------------------------------------- */
+/* Backward-Euler (SNES) form: src/fv/mpfao/tdympfao_snes.c:19-203. */
+TDyErrorCode TDySetDtimeForSNESSolver(TDy tdy, double dt);                    /* include/tdycore.h:237 */
+TDyErrorCode TDySetPreviousSolutionForSNESSolver(TDy tdy, const double *U);   /* include/tdycore.h:240 */
+TDyErrorCode TDyPreSolveSNESSolver(TDy tdy);                                 /* src/tdycore.c:2074 */
+TDyErrorCode TDyPostSolve(TDy tdy, const double *U);                         /* src/tdycore.c:2056 */
+/* TDyMPFAOSNESFunction (tdympfao_snes.c:67): R[ncells] from U[ncells]. */
+TDyErrorCode TDyMPFAOSNESFunction(TDy tdy, const double *U, double *R);
+/* TDyMPFAOSNESJacobian (tdympfao_snes.c:143): J values in pattern order. */
+TDyErrorCode TDyMPFAOSNESJacobian(TDy tdy, const double *U, double *J);
+/* Fused residual + Jacobian at the same U (one state update). */
+TDyErrorCode TDyMPFAOSNESFunctionJacobian(TDy tdy, const double *U, double *R, double *J);
+
+/* TS (implicit, IFunction/IJacobian) form: src/fv/mpfao/tdympfao_ts.c:153,520. */
+TDyErrorCode TDyMPFAOIFunction(TDy tdy, double t, const double *U, const double *U_t, double *R);
+TDyErrorCode TDyMPFAOIJacobian(TDy tdy, double t, const double *U, const double *U_t, double shift, double *J);
+TDyErrorCode TDyMPFAOIFunctionIJacobian(TDy tdy, double t, const double *U, const double *U_t, double shift,
+                                        double *R, double *J);
+
+/* Device-pointer variants (HBM-resident operands). R or J may be NULL to
+ * skip that output. stream is a cudaStream_t or NULL. */
+TDyErrorCode TDyMPFAOSNESFunctionJacobianDevice(TDy tdy, const double *dU, double *dR, double *dJ, void *stream);
+TDyErrorCode TDyMPFAOIFunctionIJacobianDevice(TDy tdy, double t, const double *dU, const double *dU_t, double shift,
+                                              double *dR, double *dJ, void *stream);
+TDyErrorCode TDyPreSolveSNESSolverDevice(TDy tdy, const double *dU_prev, void *stream);
+/* Number of hot-path kernel launches one ...Device call enqueues. */
+TDyErrorCode TDyGetLaunchesPerEvaluation(TDy tdy, int *nlaunch);
+TDyErrorCode TDySynchronize(TDy tdy);
+
+/* State and diagnostics: TDyUpdateState (src/tdycore.c:1461) and
+ * TDyGetLiquidSaturation/TDyGetLiquidMass (include/tdycore.h:213-215).
+ * Outputs are host arrays of ncells values. */
+TDyErrorCode TDyUpdateState(TDy tdy, const double *U, int ncells);
+TDyErrorCode TDyGetLiquidSaturation(TDy tdy, double *S);
+TDyErrorCode TDyGetLiquidMass(TDy tdy, double *mass);
+
+/* Setup export for test harnesses (host arrays owned by the handle); the
+ * layout is described in tdycore_gb300_setup.h. */
+struct TDyMPFAOSetupView;
+TDyErrorCode TDyMPFAOGetSetupView(TDy tdy, struct TDyMPFAOSetupView *view);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

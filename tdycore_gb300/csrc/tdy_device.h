@@ -1,0 +1,24 @@
+// tdy_device.h -- host-side interface of the CUDA translation unit.
+#pragma once
+
+#include "tdy_internal.h"
+
+namespace tdy {
+
+enum { FORM_SNES = 0, FORM_TS = 1 };
+
+int device_setup(_p_TDy *t);
+void device_destroy(_p_TDy *t);
+int device_upload_source_sink(_p_TDy *t);
+int device_presolve(_p_TDy *t, const double *dU_prev, void *stream);
+int device_presolve_host(_p_TDy *t, const double *U_prev);
+int device_eval(_p_TDy *t, int form, double time, const double *dU, const double *dUt, double shift, double *dR,
+                double *dJ, void *stream);
+int device_eval_host(_p_TDy *t, int form, double time, const double *U, const double *Ut, double shift, double *R,
+                     double *J);
+int device_launches_per_eval(_p_TDy *t);
+int device_synchronize(_p_TDy *t);
+int device_update_state_host(_p_TDy *t, const double *U);
+int device_get_diagnostic(_p_TDy *t, int which, double *out);
+
+}  // namespace tdy

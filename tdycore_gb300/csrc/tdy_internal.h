@@ -1,0 +1,180 @@
+// tdy_internal.h -- host-side data model of the GB300 MPFA-O Richards path.
+//
+// The structs here restate, for z-extruded hexahedral and prismatic meshes,
+// the parts of the reference's TDyMesh (include/private/tdymeshimpl.h:35-219)
+// and TDyMPFAO (include/private/tdympfaoimpl.h:13-117) that the residual and
+// Jacobian evaluation needs.  They are built once on the host by TDySetup and
+// uploaded to the device in flat structure-of-arrays form.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/tdycore_gb300.h"
+#include "../../include/tdycore_gb300_setup.h"
+
+namespace tdy {
+
+// Records an error message for the calling thread and returns the code.
+int set_error(int code, const char *fmt, ...);
+
+// ---------------------------------------------------------------------------
+// Options (reference: src/tdycore.c:260-296 SetDefaultOptions and
+// src/fv/mpfao/tdympfao.c:428-444 TDyCreate_MPFAO).
+struct Options {
+  double gravity = 9.8068;
+  double porosity = 0.25;
+  double permeability = 1.e-12;
+  double residual_saturation = 0.15;
+  double gardner_n = 0.5;
+  double vangenuchten_m = 0.8;
+  double vangenuchten_alpha = 1.e-4;
+  double mualem_poly_x0 = 0.995;
+  double mualem_poly_x1 = 0.99;
+  double mualem_poly_x2 = 1.00;
+  double mualem_poly_dx = 0.005;
+  int rho_type = WATER_DENSITY_CONSTANT;
+  int mu_type = WATER_VISCOSITY_CONSTANT;
+  int gmatrix_method = MPFAO_GMATRIX_DEFAULT;
+  int bc_type = DIRICHLET_BC;
+  double Pref = 101325.0;
+  double Tref = 25.0;
+  bool has_pressure_bc_value = false;
+  double pressure_bc_value = 0.0;
+};
+
+// How a per-cell property is specified by the user.
+struct ScalarSpec {
+  enum Kind { DEFAULT, CONSTANT, FUNCTION } kind = DEFAULT;
+  double value = 0.0;
+  TDyScalarSpatialFunction func = nullptr;
+  std::vector<std::pair<int, double>> overrides;  // per-cell values
+};
+
+struct PermSpec {
+  enum Kind { DEFAULT, ISO_CONST, DIAG_CONST, TENSOR_CONST, ISO_FUNC, DIAG_FUNC, TENSOR_FUNC } kind = DEFAULT;
+  double k[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  void (*func)(int, double *, double *) = nullptr;
+  std::vector<std::pair<int, std::vector<double>>> overrides;
+};
+
+// ---------------------------------------------------------------------------
+// Mesh input: a surface mesh extruded in z.
+struct ExtrudedInput {
+  bool set = false;
+  int nv2 = 0, nc2 = 0, nvpc = 0, nlayers = 0;
+  std::vector<double> xy;      // 2*nv2
+  std::vector<int> cells2d;    // nvpc*nc2, counter-clockwise
+  std::vector<double> z;       // (nlayers+1)*nv2
+};
+
+// Unstructured 3-D mesh with the connectivity the MPFA-O setup needs.
+struct Mesh {
+  int nv = 0, nc = 0, nf = 0, nb = 0;
+  std::vector<double> vx;                        // 3*nv vertex coordinates
+  std::vector<int> cell_vert_off, cell_verts;    // cell -> vertices
+  std::vector<int> cell_face_off, cell_faces;    // cell -> faces
+  std::vector<double> cell_cen, cell_vol;        // 3*nc, nc
+  std::vector<int> face_vert_off, face_verts;    // face -> vertices (oriented)
+  std::vector<int> face_cell0, face_cell1;       // reference encoding (<0 -> boundary -(b+1))
+  std::vector<double> face_cen, face_nrm, face_area;
+  std::vector<int> face_bnd;                     // boundary index or -1
+  std::vector<int> bnd_face;                     // nb -> face id
+  std::vector<int> vert_cell_off, vert_cells;    // vertex -> cells (ascending)
+  std::vector<int> vert_face_off, vert_faces;    // vertex -> faces (internal first, ascending)
+};
+
+// Builds the z-extruded mesh: connectivity, geometry and face orientation.
+int build_extruded_mesh(const ExtrudedInput &in, Mesh &m);
+
+// ---------------------------------------------------------------------------
+// Cell material and characteristic-curve parameters (SoA).
+struct Materials {
+  std::vector<double> K0;          // 9*nc
+  std::vector<double> porosity;    // nc
+  std::vector<double> Sr;          // nc
+  std::vector<int> sat_type;       // nc
+  std::vector<double> sat_param;   // 3*nc
+  std::vector<int> relperm_type;   // nc
+  std::vector<double> relperm_param;  // 9*nc
+  std::vector<double> source_sink; // nc
+};
+
+// Per-boundary-face condition data.
+struct Boundary {
+  std::vector<int> type;           // nb
+  std::vector<int> has_value;      // nb
+  std::vector<double> value;       // nb
+  std::vector<double> rho, vis;    // nb (EOS at Pref)
+};
+
+// Result of the MPFA-O setup (host copy; also the layout uploaded to HBM).
+struct MPFAOSetup {
+  int nrows = 0, ncols = 0;
+  long long ntrans = 0;
+  std::vector<int> v_row_off, v_col_off, v_nint;  // nv+1, nv+1, nv
+  std::vector<long long> v_trans_off;             // nv+1
+  std::vector<int> row_face;                      // nrows
+  std::vector<int> row_lup, row_ldn;              // nrows: local internal-cell index or -1
+  std::vector<int> col_ext;                       // ncols
+  std::vector<double> trans;                      // ntrans
+  std::vector<double> gravdis;                    // nf
+  // Jacobian pattern
+  std::vector<int> rowptr, colidx;
+  // cell -> (vertex, local index, slot map) gather program
+  std::vector<int> cv_off;         // nc+1
+  std::vector<int> cv_vertex;      // per (cell, vertex)
+  std::vector<int> cv_local;       // local internal-cell index of the cell at that vertex
+  std::vector<int> cv_slot_off;    // offset into cv_slots for this (cell, vertex)
+  std::vector<uint8_t> cv_slots;   // CSR slot (within the row) of each internal column
+  std::vector<long long> v_jv_off; // nv+1: scratch offsets (nint*nint + nint doubles)
+  int max_nint = 0, max_nrow = 0, max_ncol = 0, max_row_nnz = 0;
+};
+
+int mpfao_setup(const Options &opt, const Mesh &m, const Materials &mat, const Boundary &bnd, MPFAOSetup &s);
+
+// EOS at one pressure (src/materials/tdyeos.c:5-136).
+void eos_density(int type, double p, double *rho, double *drho, double *d2rho);
+void eos_viscosity(int type, double p, double *vis, double *dvis, double *d2vis);
+// Mualem cubic smoothing coefficients (tdycharacteristiccurves.c:577-596).
+int mualem_smoothing_coeffs(double m, double x0, double x1, double x2, double dx, double coeffs[4]);
+
+struct DeviceState;  // defined in the CUDA translation unit
+
+}  // namespace tdy
+
+// ---------------------------------------------------------------------------
+// The handle.
+struct _p_TDy {
+  unsigned flags = 0;
+  int mode = RICHARDS;
+  int discretization = MPFA_O;
+  tdy::Options opt;
+  tdy::ExtrudedInput mesh_in;
+  tdy::ScalarSpec porosity, sr;
+  tdy::PermSpec perm;
+  std::vector<std::pair<int, std::vector<double>>> vg_over, gardner_over;
+  std::vector<std::pair<int, double>> mualem_over, irmay_over;
+  std::vector<std::pair<int, double>> source_over;
+  TDyScalarSpatialFunction bc_pressure_func = nullptr;
+  TDyScalarSpatialIntegerFunction bc_type_func = nullptr;
+
+  // built by TDySetup
+  bool is_setup = false;
+  tdy::Mesh mesh;
+  tdy::Materials mat;
+  tdy::Boundary bnd;
+  tdy::MPFAOSetup setup;
+  double dtime = 0.0;
+  bool have_prev = false;
+  std::vector<double> U_prev;
+  tdy::DeviceState *dev = nullptr;
+};
+
+enum : unsigned {
+  TDY_FLAG_MODE = 1u << 1,
+  TDY_FLAG_DISC = 1u << 2,
+  TDY_FLAG_OPTIONS = 1u << 3,
+  TDY_FLAG_SETUP = 1u << 4,
+};

@@ -1,0 +1,634 @@
+// tdy_kernels.cu -- sm_103a kernels of the MPFA-O Richards residual and
+// Jacobian, and their host-side launch code.
+//
+// One evaluation is three launches on one stream:
+//   1. state_kernel   (cells, then boundary faces)
+//        TDyUpdateState_Richards_MPFAO (src/fv/mpfao/tdympfao.c:2527-2594),
+//        TDyMPFAO_SetBoundaryPressure + TDyMPFAOUpdateBoundaryState
+//        (src/fv/mpfao/tdympfao_utils.c:24-99, 690-759) and the accumulation
+//        terms of TDyMPFAOSNESFunction/Jacobian (tdympfao_snes.c:19-30,
+//        112-123, 166-179) or TDyMPFAOIFunction/IJacobian_Accumulation
+//        (tdympfao_ts.c:191-212, 459-517).
+//   2. vertex_kernel  (one thread per vertex)
+//        MatMult(Trans_mat, P_vec) (tdympfao_ts.c:184) restricted to the
+//        vertex's rows, the upwinded flux of TDyMPFAOIFunction_Vertices
+//        (tdympfao_ts.c:12-150) and the Jacobian entries of
+//        TDyMPFAOIJacobian_Vertices (tdympfao_ts.c:235-456).  Each vertex
+//        writes its partial residual R_v[nint] and partial Jacobian block
+//        J_v[nint][nint] (rows and columns: the vertex's internal cells) to a
+//        scratch area it alone owns.
+//   3. cell_kernel    (one thread per cell)
+//        sums, in a fixed order, the partials of the cell's vertices into
+//        R[cell] and into the cell's row of the fixed CSR pattern, then adds
+//        the accumulation terms.  No atomics: results are bitwise
+//        reproducible run to run.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <type_traits>
+#include <vector>
+
+#include "tdy_device.h"
+
+namespace tdy {
+
+#define TDY_MAX_ROWS 64
+#define TDY_MAX_NINT 64
+#define TDY_MAX_ROW_NNZ 64
+
+struct DevArgs {
+  int nc, nb, nv;
+  int form;
+  int rho_type, mu_type;
+  int needR, needJ;
+  double Pref, dt, shift;
+  // inputs
+  const double *U, *Ut;
+  // cells
+  const double *vol, *poro, *Sr, *sat_param, *rp_param, *ss, *accum_prev;
+  const int *sat_type, *rp_type;
+  // boundary faces
+  const int *bnd_cell, *bnd_type, *bnd_has;
+  const double *bnd_val, *bnd_rho, *bnd_vis;
+  // extended state (cells then boundary faces)
+  double *P, *rho, *drho, *lam, *dlam;
+  unsigned char *seep;
+  double *acc_a, *acc_b, *jdiag;
+  // faces
+  const int *f_up, *f_dn;
+  const double *G;
+  // vertices
+  const int *v_row_off, *v_col_off, *v_nint;
+  const long long *v_trans_off, *v_jv_off;
+  const int *row_face, *row_lup, *row_ldn, *col_ext;
+  const double *trans;
+  double *scratch;
+  // cell gather
+  const int *rowptr, *cv_off, *cv_vertex, *cv_local, *cv_slot_off;
+  const unsigned char *cv_slots;
+  // outputs
+  double *R, *J;
+};
+
+struct DeviceState {
+  cudaStream_t stream = nullptr;
+  DevArgs a;
+  // owned allocations
+  std::vector<void *> allocs;
+  double *dU = nullptr, *dUt = nullptr, *dR = nullptr, *dJ = nullptr;
+  double *diagS = nullptr, *diagMass = nullptr;
+  int nnz = 0;
+};
+
+#define CUDA_TRY(call)                                                                          \
+  do {                                                                                          \
+    cudaError_t e_ = (call);                                                                    \
+    if (e_ != cudaSuccess)                                                                      \
+      return set_error(TDY_ERR_GPU, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// Constitutive relations, restated from src/materials/tdycharacteristiccurves.c
+// and src/materials/tdyeos.c with the reference's operation order.
+
+// PressureSaturation_VanGenuchten (tdycharacteristiccurves.c:692-717) and
+// PressureSaturation_Gardner (:641-667).
+__device__ __forceinline__ void saturation(int type, const double *par, double Sr, double Pc, double *S, double *dS,
+                                           double *d2S) {
+  if (type == SAT_FUNC_VAN_GENUCHTEN) {
+    const double m = par[0], alpha = par[1];
+    if (Pc <= 0) {
+      *S = 1;
+      *dS = 0;
+      *d2S = 0.0;
+    } else {
+      double n = 1 / (1 - m);
+      double pc_alpha = Pc * alpha;
+      double pc_alpha_n = pow(pc_alpha, n);
+      double one_plus = 1 + pc_alpha_n;
+      double Se = pow(one_plus, -m);
+      *S = (1.0 - Sr) * Se + Sr;
+      double dSe_dPc = -m * n * alpha * pc_alpha_n / (pc_alpha * pow(one_plus, m + 1));
+      *dS = -dSe_dPc * (1.0 - Sr);
+      double d2Se = m * n * (pc_alpha_n)*pow(one_plus, -m - 2.0) * ((m * n + 1.0) * pc_alpha_n - n + 1) / (Pc * Pc);
+      *d2S = (1.0 - Sr) * d2Se;
+    }
+  } else {
+    const double m = par[1], alpha = par[2];
+    if (Pc < 0) {
+      *S = 1;
+      *dS = 0;
+      *d2S = 0.0;
+    } else {
+      double Se = exp(-alpha * Pc / m);
+      *S = (1.0 - Sr) * Se + Sr;
+      double dSe_dPc = -alpha / m * exp(-alpha * Pc / m);
+      *dS = -dSe_dPc * (1.0 - Sr);
+      double d2Se = -alpha / m * dSe_dPc;
+      *d2S = (1.0 - Sr) * d2Se;
+    }
+  }
+}
+
+// RelativePermeability_Mualem (tdycharacteristiccurves.c:468-485, 551-562,
+// 607-614) and RelativePermeability_Irmay (:451-460).
+__device__ __forceinline__ void relperm(int type, const double *p, double Se, double *Kr, double *dKr) {
+  if (type == REL_PERM_FUNC_MUALEM) {
+    const double m = p[0], x0 = p[1], x1 = p[2], dx = p[4];
+    if (Se > x1) {
+      double xt = (Se - x0) / dx;
+      *Kr = p[5] + xt * (p[6] + xt * (p[7] + xt * p[8]));
+      *dKr = (p[6] + xt * (2.0 * p[7] + xt * 3.0 * p[8])) / dx;
+    } else {
+      *Kr = 1.0;
+      *dKr = 0.0;
+      if (Se >= 1.0) return;
+      double so = pow(Se, 1 / m);
+      double tmp = pow(1 - so, m);
+      double kr = sqrt(Se);
+      kr *= (1 - tmp) * (1 - tmp);
+      *Kr = kr;
+      double d = 0.5 * kr / Se;
+      d += 2 * pow(Se, 1 / m - 0.5) * pow(1 - so, m - 1) * (1 - pow(1 - so, m));
+      *dKr = d;
+    }
+  } else {
+    const double m = p[0];
+    *Kr = 1.0;
+    *dKr = 0.0;
+    if (Se >= 1.0) return;
+    *Kr = pow(Se, m);
+    *dKr = pow(Se, m - 1) * m;
+  }
+}
+
+// EOSComputeWaterDensity / EOSComputeWaterViscosity (tdyeos.c:5-136) at
+// T = Tref and zero salinity.
+__device__ __forceinline__ void density(int type, double p, double *rho, double *drho, double *d2rho) {
+  if (type == WATER_DENSITY_CONSTANT) {
+    *rho = 998.0;
+    *drho = 0.0;
+    *d2rho = 0.0;
+  } else if (type == WATER_DENSITY_EXPONENTIAL) {
+    if (p < 101325.e0) {
+      *rho = 997.16e0;
+      *drho = 0.0;
+      *d2rho = 0.0;
+    } else {
+      double r = 997.16e0 * exp(1.e-8 * (p - 101325.e0));
+      *rho = r;
+      *drho = 1.e-8 * r;
+      *d2rho = 1.e-8 * (1.e-8 * r);
+    }
+  } else {
+    const double T = 25.0, P = p * 1.e-6;
+    double pw = 1 + 1.e-6 * (-80. * T - 3.3 * (T * T) + 0.00175 * (T * T * T) + 489. * P - 2. * T * P +
+                             0.016 * P * (T * T) - 1.3e-5 * (T * T * T) * P - 0.333 * (P * P) - 0.002 * T * (P * P));
+    *rho = pw * 1000.;
+    *drho = 0.0;
+    *d2rho = 0.0;
+  }
+}
+
+__device__ __forceinline__ void viscosity(int type, double *vis, double *dvis) {
+  if (type == WATER_VISCOSITY_CONSTANT) {
+    *vis = 9.94e-4;
+  } else {
+    const double T = 25.0;
+    *vis = (0.1 + 1.65 * exp((-0.42 * (0.17 * 0.17) + 0.045) * pow(T, 0.8))) * 1e-3;
+  }
+  *dvis = 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// 1. cell and boundary-face state
+__global__ void __launch_bounds__(256) state_kernel(DevArgs a) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < a.nc) {
+    const double U = a.U[i];
+    const double Sr = a.Sr[i];
+    const double Pc = a.Pref - U;
+    double S, dS, d2S;
+    saturation(a.sat_type[i], a.sat_param + 3 * (size_t)i, Sr, Pc, &S, &dS, &d2S);
+    double Se = (S - Sr) / (1.0 - Sr);
+    double Kr, dKr_dSe;
+    relperm(a.rp_type[i], a.rp_param + 9 * (size_t)i, Se, &Kr, &dKr_dSe);
+    double dSe_dS = 1.0 / (1.0 - Sr);
+    double dKr_dS = dKr_dSe * dSe_dS;
+    double P = a.Pref - Pc;
+    double rho, drho, d2rho, vis, dvis;
+    density(a.rho_type, P, &rho, &drho, &d2rho);
+    viscosity(a.mu_type, &vis, &dvis);
+    a.P[i] = P;
+    a.rho[i] = rho;
+    a.drho[i] = drho;
+    a.lam[i] = Kr / vis;
+    a.dlam[i] = dKr_dS * dS / vis - Kr / (vis * vis) * dvis;
+    a.seep[i] = 0;
+    const double poro = a.poro[i], vol = a.vol[i];
+    const double dporo = 0.0;
+    double dmass = rho * dporo * S + drho * poro * S + rho * poro * dS;
+    if (a.form == FORM_SNES) {
+      double acc = rho * poro * S * vol / a.dt;
+      a.acc_a[i] = acc - a.accum_prev[i];
+      a.acc_b[i] = a.ss[i];
+      a.jdiag[i] = dmass * vol * (1.0 / a.dt);
+    } else {
+      const double Ut = a.Ut[i];
+      const double d2poro = 0.0;
+      double d2mass = (dS * rho * dporo + S * drho * dporo + S * rho * d2poro + dS * drho * poro + S * d2rho * poro +
+                       S * drho * dporo + d2S * rho * poro + dS * drho * poro + dS * rho * dporo);
+      a.acc_a[i] = dmass * Ut * vol;
+      a.acc_b[i] = a.ss[i] * vol;
+      a.jdiag[i] = (a.shift * dmass + d2mass * Ut) * vol;
+    }
+  } else if (i < a.nc + a.nb) {
+    const int b = i - a.nc;
+    const int c = a.bnd_cell[b];
+    const double p = a.bnd_has[b] ? a.bnd_val[b] : a.U[c];
+    const double Sr = a.Sr[c];
+    double S, dS, d2S;
+    saturation(a.sat_type[c], a.sat_param + 3 * (size_t)c, Sr, a.Pref - p, &S, &dS, &d2S);
+    double Se = (S - Sr) / (1.0 - Sr);
+    double Kr, dKr;
+    relperm(a.rp_type[c], a.rp_param + 9 * (size_t)c, Se, &Kr, &dKr);
+    a.P[i] = p;
+    a.rho[i] = a.bnd_rho[b];
+    a.drho[i] = 0.0;
+    a.lam[i] = Kr / a.bnd_vis[b];
+    a.dlam[i] = 0.0;
+    a.seep[i] = (a.bnd_type[b] == SEEPAGE_BC && p <= a.Pref) ? 1 : 0;
+  }
+}
+
+// Accumulation at the previous solution (TDyMPFAOSNESPreSolve,
+// tdympfao_snes.c:19-64).
+__global__ void __launch_bounds__(256) presolve_kernel(DevArgs a, const double *Uprev, double *accum_prev) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.nc) return;
+  const double Sr = a.Sr[i];
+  const double Pc = a.Pref - Uprev[i];
+  double S, dS, d2S;
+  saturation(a.sat_type[i], a.sat_param + 3 * (size_t)i, Sr, Pc, &S, &dS, &d2S);
+  double rho, drho, d2rho;
+  density(a.rho_type, a.Pref - Pc, &rho, &drho, &d2rho);
+  accum_prev[i] = rho * a.poro[i] * S * a.vol[i] / a.dt;
+}
+
+// Diagnostics (TDyUpdateDiagnostics_MPFAO, tdympfao.c:2780-2806): saturation
+// and rho*V per cell.
+__global__ void __launch_bounds__(256) diag_kernel(DevArgs a, double *Sout, double *mass) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.nc) return;
+  const double Sr = a.Sr[i];
+  const double Pc = a.Pref - a.U[i];
+  double S, dS, d2S;
+  saturation(a.sat_type[i], a.sat_param + 3 * (size_t)i, Sr, Pc, &S, &dS, &d2S);
+  double rho, drho, d2rho;
+  density(a.rho_type, a.Pref - Pc, &rho, &drho, &d2rho);
+  Sout[i] = S;
+  mass[i] = rho * a.vol[i];
+}
+
+// ---------------------------------------------------------------------------
+// 2. per-vertex flux and Jacobian partials
+__global__ void __launch_bounds__(128) vertex_kernel(DevArgs a) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= a.nv) return;
+  const int nint = a.v_nint[v];
+  if (nint == 0) return;
+  const int r0 = a.v_row_off[v], nrow = a.v_row_off[v + 1] - r0;
+  const int c0 = a.v_col_off[v], ncol = a.v_col_off[v + 1] - c0;
+  const double *T = a.trans + a.v_trans_off[v];
+  double *Jv = a.scratch + a.v_jv_off[v];
+  double *Rv = Jv + nint * nint;
+
+  double w[TDY_MAX_ROWS], Eu[TDY_MAX_ROWS], Ed[TDY_MAX_ROWS], fl[TDY_MAX_ROWS];
+  for (int r = 0; r < nrow; r++) {
+    const double *Tr = T + (size_t)r * ncol;
+    double TP = 0.0;
+    for (int c = 0; c < ncol; c++) TP += Tr[c] * a.P[a.col_ext[c0 + c]];
+    const int f = a.row_face[r0 + r];
+    const int up = a.f_up[f], dn = a.f_dn[f];
+    const double G = a.G[f];
+    const double den = (a.rho[up] + a.rho[dn]) * 0.5;
+    const bool flowdn = (TP + den * G < 0.0);
+    const int u = flowdn ? up : dn;
+    const double ukvr = a.lam[u];
+    const bool zero = a.seep[u] != 0;
+    double fluxm = 0.0;
+    if (!zero) {
+      fluxm = den * ukvr * (-TP);
+      fluxm += -(den * den) * ukvr * G;
+    }
+    fl[r] = fluxm;
+    if (a.needJ) {
+      if (zero) {
+        w[r] = 0.0;
+        Eu[r] = 0.0;
+        Ed[r] = 0.0;
+      } else {
+        const double dden_up = 0.5 * a.drho[up], dden_dn = 0.5 * a.drho[dn];
+        const double dukvr_up = flowdn ? a.dlam[up] : 0.0;
+        const double dukvr_dn = flowdn ? 0.0 : a.dlam[dn];
+        w[r] = den * ukvr;
+        Eu[r] = dden_up * ukvr * TP + den * dukvr_up * TP + (2 * den * dden_up * ukvr * G + (den * den) * dukvr_up * G);
+        Ed[r] = dden_dn * ukvr * TP + den * dukvr_dn * TP + (2 * den * dden_dn * ukvr * G + (den * den) * dukvr_dn * G);
+      }
+    }
+  }
+  if (a.needR) {
+    for (int c = 0; c < nint; c++) {
+      double s = 0.0;
+      for (int r = 0; r < nrow; r++) {
+        if (a.row_lup[r0 + r] == c) s += fl[r];
+        if (a.row_ldn[r0 + r] == c) s -= fl[r];
+      }
+      Rv[c] = s;
+    }
+  }
+  if (a.needJ) {
+    int lst[TDY_MAX_ROWS];
+    for (int c = 0; c < nint; c++) {
+      int nl = 0;
+      for (int r = 0; r < nrow; r++) {
+        if (a.row_lup[r0 + r] == c) lst[nl++] = r;
+        if (a.row_ldn[r0 + r] == c) lst[nl++] = -(r + 1);
+      }
+      for (int b = 0; b < nint; b++) {
+        double acc = 0.0;
+        for (int k = 0; k < nl; k++) {
+          const bool is_up = lst[k] >= 0;
+          const int r = is_up ? lst[k] : -lst[k] - 1;
+          double jac = w[r] * T[(size_t)r * ncol + b];
+          if (a.row_lup[r0 + r] == b) jac += Eu[r];
+          if (a.row_ldn[r0 + r] == b) jac += Ed[r];
+          jac = -jac;
+          acc += is_up ? jac : -jac;
+        }
+        Jv[c * nint + b] = acc;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// 3. per-cell deterministic gather into R and the CSR row
+__global__ void __launch_bounds__(128) cell_kernel(DevArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.nc) return;
+  const int k0 = a.cv_off[i], k1 = a.cv_off[i + 1];
+  if (a.needR) {
+    double s = 0.0;
+    for (int k = k0; k < k1; k++) {
+      const int v = a.cv_vertex[k];
+      const int nint = a.v_nint[v];
+      s += a.scratch[a.v_jv_off[v] + (long long)nint * nint + a.cv_local[k]];
+    }
+    s += a.acc_a[i];
+    s -= a.acc_b[i];
+    a.R[i] = s;
+  }
+  if (a.needJ) {
+    const int p0 = a.rowptr[i], rn = a.rowptr[i + 1] - p0;
+    double row[TDY_MAX_ROW_NNZ];
+    for (int j = 0; j < rn; j++) row[j] = 0.0;
+    int diag = -1;
+    for (int k = k0; k < k1; k++) {
+      const int v = a.cv_vertex[k];
+      const int nint = a.v_nint[v];
+      const double *blk = a.scratch + a.v_jv_off[v] + (long long)a.cv_local[k] * nint;
+      const unsigned char *sl = a.cv_slots + a.cv_slot_off[k];
+      for (int b = 0; b < nint; b++) row[sl[b]] += blk[b];
+      diag = sl[a.cv_local[k]];
+    }
+    if (diag >= 0) row[diag] += a.jdiag[i];
+    double *out = a.J + p0;
+    for (int j = 0; j < rn; j++) out[j] = row[j];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+
+template <class T>
+static int dalloc(DeviceState *d, T **p, size_t n) {
+  *p = nullptr;
+  if (n == 0) n = 1;
+  cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
+  if (e != cudaSuccess) return set_error(TDY_ERR_GPU, "cudaMalloc(%zu bytes): %s", n * sizeof(T), cudaGetErrorString(e));
+  d->allocs.push_back(*p);
+  return 0;
+}
+
+template <class T>
+static int dupload(DeviceState *d, T **p, const std::vector<T> &h) {
+  int ierr = dalloc(d, p, h.size());
+  if (ierr) return ierr;
+  if (!h.empty()) CUDA_TRY(cudaMemcpy(*p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return 0;
+}
+
+int device_setup(_p_TDy *t) {
+  const Mesh &m = t->mesh;
+  const MPFAOSetup &s = t->setup;
+  if (s.max_nrow > TDY_MAX_ROWS || s.max_nint > TDY_MAX_NINT || s.max_row_nnz > TDY_MAX_ROW_NNZ)
+    return set_error(TDY_ERR_SUP, "mesh exceeds kernel limits (rows/vertex %d, cells/vertex %d, row nnz %d; max %d)",
+                     s.max_nrow, s.max_nint, s.max_row_nnz, TDY_MAX_ROWS);
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0)
+    return set_error(TDY_ERR_GPU, "no CUDA device available: %s", e != cudaSuccess ? cudaGetErrorString(e) : "0 devices");
+  DeviceState *d = new DeviceState();
+  t->dev = d;
+  CUDA_TRY(cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking));
+  DevArgs &a = d->a;
+  memset(&a, 0, sizeof(a));
+  a.nc = m.nc;
+  a.nb = m.nb;
+  a.nv = m.nv;
+  a.Pref = t->opt.Pref;
+  a.rho_type = t->opt.rho_type;
+  a.mu_type = t->opt.mu_type;
+  const int next = m.nc + m.nb;
+  int ierr = 0;
+#define UP(ptr, vec)                                                           \
+  do {                                                                         \
+    decltype(vec) const &v_ = (vec);                                           \
+    using E_ = typename std::remove_const<typename std::remove_reference<decltype(v_[0])>::type>::type; \
+    E_ *p_;                                                                    \
+    if ((ierr = dupload(d, &p_, v_))) return ierr;                             \
+    ptr = p_;                                                                  \
+  } while (0)
+  UP(a.vol, m.cell_vol);
+  UP(a.poro, t->mat.porosity);
+  UP(a.Sr, t->mat.Sr);
+  UP(a.sat_param, t->mat.sat_param);
+  UP(a.rp_param, t->mat.relperm_param);
+  UP(a.ss, t->mat.source_sink);
+  UP(a.sat_type, t->mat.sat_type);
+  UP(a.rp_type, t->mat.relperm_type);
+  std::vector<int> bnd_cell(m.nb);
+  for (int b = 0; b < m.nb; b++) bnd_cell[b] = m.face_cell1[m.bnd_face[b]];
+  UP(a.bnd_cell, bnd_cell);
+  UP(a.bnd_type, t->bnd.type);
+  UP(a.bnd_has, t->bnd.has_value);
+  UP(a.bnd_val, t->bnd.value);
+  UP(a.bnd_rho, t->bnd.rho);
+  UP(a.bnd_vis, t->bnd.vis);
+  std::vector<int> fup(m.nf), fdn(m.nf);
+  for (int f = 0; f < m.nf; f++) {
+    int u = m.face_cell0[f], w = m.face_cell1[f];
+    fup[f] = u >= 0 ? u : m.nc + (-u - 1);
+    fdn[f] = w >= 0 ? w : m.nc + (-w - 1);
+  }
+  UP(a.f_up, fup);
+  UP(a.f_dn, fdn);
+  UP(a.G, s.gravdis);
+  UP(a.v_row_off, s.v_row_off);
+  UP(a.v_col_off, s.v_col_off);
+  UP(a.v_nint, s.v_nint);
+  UP(a.v_trans_off, s.v_trans_off);
+  UP(a.v_jv_off, s.v_jv_off);
+  UP(a.row_face, s.row_face);
+  UP(a.row_lup, s.row_lup);
+  UP(a.row_ldn, s.row_ldn);
+  UP(a.col_ext, s.col_ext);
+  UP(a.trans, s.trans);
+  UP(a.rowptr, s.rowptr);
+  UP(a.cv_off, s.cv_off);
+  UP(a.cv_vertex, s.cv_vertex);
+  UP(a.cv_local, s.cv_local);
+  UP(a.cv_slot_off, s.cv_slot_off);
+  UP(a.cv_slots, s.cv_slots);
+#undef UP
+  double *p;
+  if ((ierr = dalloc(d, &a.P, next))) return ierr;
+  if ((ierr = dalloc(d, &a.rho, next))) return ierr;
+  if ((ierr = dalloc(d, &a.drho, next))) return ierr;
+  if ((ierr = dalloc(d, &a.lam, next))) return ierr;
+  if ((ierr = dalloc(d, &a.dlam, next))) return ierr;
+  if ((ierr = dalloc(d, &a.seep, next))) return ierr;
+  if ((ierr = dalloc(d, &a.acc_a, m.nc))) return ierr;
+  if ((ierr = dalloc(d, &a.acc_b, m.nc))) return ierr;
+  if ((ierr = dalloc(d, &a.jdiag, m.nc))) return ierr;
+  if ((ierr = dalloc(d, &p, m.nc))) return ierr;
+  CUDA_TRY(cudaMemset(p, 0, sizeof(double) * m.nc));
+  a.accum_prev = p;
+  if ((ierr = dalloc(d, &a.scratch, (size_t)s.v_jv_off[m.nv]))) return ierr;
+  d->nnz = (int)s.colidx.size();
+  if ((ierr = dalloc(d, &d->dU, m.nc))) return ierr;
+  if ((ierr = dalloc(d, &d->dUt, m.nc))) return ierr;
+  if ((ierr = dalloc(d, &d->dR, m.nc))) return ierr;
+  if ((ierr = dalloc(d, &d->dJ, d->nnz))) return ierr;
+  if ((ierr = dalloc(d, &d->diagS, m.nc))) return ierr;
+  if ((ierr = dalloc(d, &d->diagMass, m.nc))) return ierr;
+  CUDA_TRY(cudaDeviceSynchronize());
+  return 0;
+}
+
+void device_destroy(_p_TDy *t) {
+  DeviceState *d = t->dev;
+  if (!d) return;
+  if (d->stream) cudaStreamSynchronize(d->stream);
+  for (void *p : d->allocs) cudaFree(p);
+  if (d->stream) cudaStreamDestroy(d->stream);
+  delete d;
+  t->dev = nullptr;
+}
+
+int device_upload_source_sink(_p_TDy *t) {
+  DeviceState *d = t->dev;
+  CUDA_TRY(cudaMemcpy((void *)d->a.ss, t->mat.source_sink.data(), sizeof(double) * t->mesh.nc, cudaMemcpyHostToDevice));
+  return 0;
+}
+
+static inline unsigned nblocks(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+int device_presolve(_p_TDy *t, const double *dUprev, void *stream) {
+  DeviceState *d = t->dev;
+  cudaStream_t st = stream ? (cudaStream_t)stream : d->stream;
+  DevArgs a = d->a;
+  a.dt = t->dtime;
+  presolve_kernel<<<nblocks(a.nc, 256), 256, 0, st>>>(a, dUprev, (double *)a.accum_prev);
+  CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+int device_presolve_host(_p_TDy *t, const double *Uprev) {
+  DeviceState *d = t->dev;
+  CUDA_TRY(cudaMemcpyAsync(d->dU, Uprev, sizeof(double) * t->mesh.nc, cudaMemcpyHostToDevice, d->stream));
+  int ierr = device_presolve(t, d->dU, d->stream);
+  if (ierr) return ierr;
+  CUDA_TRY(cudaStreamSynchronize(d->stream));
+  return 0;
+}
+
+int device_eval(_p_TDy *t, int form, double time, const double *dU, const double *dUt, double shift, double *dR,
+                double *dJ, void *stream) {
+  (void)time;
+  DeviceState *d = t->dev;
+  cudaStream_t st = stream ? (cudaStream_t)stream : d->stream;
+  if (form == FORM_SNES && !(t->dtime > 0.0))
+    return set_error(TDY_ERR_USER, "SNES form needs TDySetDtimeForSNESSolver before evaluation");
+  DevArgs a = d->a;
+  a.form = form;
+  a.U = dU;
+  a.Ut = dUt;
+  a.dt = t->dtime;
+  a.shift = shift;
+  a.needR = dR != nullptr;
+  a.needJ = dJ != nullptr;
+  a.R = dR;
+  a.J = dJ;
+  state_kernel<<<nblocks(a.nc + a.nb, 256), 256, 0, st>>>(a);
+  vertex_kernel<<<nblocks(a.nv, 128), 128, 0, st>>>(a);
+  cell_kernel<<<nblocks(a.nc, 128), 128, 0, st>>>(a);
+  CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+int device_eval_host(_p_TDy *t, int form, double time, const double *U, const double *Ut, double shift, double *R,
+                     double *J) {
+  DeviceState *d = t->dev;
+  const size_t n = (size_t)t->mesh.nc;
+  CUDA_TRY(cudaMemcpyAsync(d->dU, U, sizeof(double) * n, cudaMemcpyHostToDevice, d->stream));
+  if (Ut) CUDA_TRY(cudaMemcpyAsync(d->dUt, Ut, sizeof(double) * n, cudaMemcpyHostToDevice, d->stream));
+  int ierr = device_eval(t, form, time, d->dU, Ut ? d->dUt : nullptr, shift, R ? d->dR : nullptr, J ? d->dJ : nullptr,
+                         d->stream);
+  if (ierr) return ierr;
+  if (R) CUDA_TRY(cudaMemcpyAsync(R, d->dR, sizeof(double) * n, cudaMemcpyDeviceToHost, d->stream));
+  if (J) CUDA_TRY(cudaMemcpyAsync(J, d->dJ, sizeof(double) * d->nnz, cudaMemcpyDeviceToHost, d->stream));
+  CUDA_TRY(cudaStreamSynchronize(d->stream));
+  return 0;
+}
+
+int device_launches_per_eval(_p_TDy *t) {
+  (void)t;
+  return 3;
+}
+
+int device_synchronize(_p_TDy *t) {
+  CUDA_TRY(cudaStreamSynchronize(t->dev->stream));
+  return 0;
+}
+
+int device_update_state_host(_p_TDy *t, const double *U) {
+  DeviceState *d = t->dev;
+  CUDA_TRY(cudaMemcpyAsync(d->dU, U, sizeof(double) * t->mesh.nc, cudaMemcpyHostToDevice, d->stream));
+  DevArgs a = d->a;
+  a.U = d->dU;
+  diag_kernel<<<nblocks(a.nc, 256), 256, 0, d->stream>>>(a, d->diagS, d->diagMass);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaStreamSynchronize(d->stream));
+  return 0;
+}
+
+int device_get_diagnostic(_p_TDy *t, int which, double *out) {
+  DeviceState *d = t->dev;
+  CUDA_TRY(cudaMemcpy(out, which == 0 ? d->diagS : d->diagMass, sizeof(double) * t->mesh.nc, cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+}  // namespace tdy
