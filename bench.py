@@ -1,0 +1,362 @@
+"""Benchmark: MPFA-O Richards fused residual + Jacobian (F+J) on GB300.
+
+One step = one TDyMPFAOSNESFunction + TDyMPFAOSNESJacobian evaluation (the
+per-Newton-iteration work of the reference's SNES callbacks) over the
+60x220x85 jittered-hex workload (SPE10 model-2 grid, seeded synthetic fields;
+see tdycore_gb300/workloads.py).  Inputs (~1.9 GB of setup arrays, the
+1.12 M-cell state) are larger than the 129 MB L2, so no flush is needed
+between iterations.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Prints one JSON line on rank 0.  --impl reference times the CPU restatement
+of the reference's F+J (the reference itself needs PETSc/MPI and cannot be
+built here) on the host cores with all available threads.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "MPFA-O F+J cells/s (% HBM peak); batched solves/s, p99 latency @1e-8 resid"
+UNIT = "cells/s"
+FALLBACK_HBM_GBS = 6800.0
+DT = 1800.0
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            d = json.loads(p.read_text())
+            for k in ("hbm_gbs", "hbm_GBs", "hbm"):
+                if k in d:
+                    return float(d[k]), "measured"
+        except Exception:
+            pass
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.gpu)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[4:8]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def build_workload(host_only=False):
+    import tdycore_gb300 as T
+    from tdycore_gb300.workloads import spe10_like
+
+    T.options_clear()
+    t0 = time.perf_counter()
+    t, U, info = spe10_like()
+    t.setup(host_only=host_only)
+    log(f"setup: {info['workload']} {t.ncells} cells, nnz {t.nnz}, {time.perf_counter() - t0:.1f} s")
+    rng = np.random.default_rng(20261203)
+    Uprev = U + rng.normal(0.0, 200.0, U.size)
+    return t, U, Uprev, info
+
+
+def algorithmic_bytes(view):
+    """Per-evaluation FP64 payload (index arrays excluded):
+    8 * (sum_v R_v C_v  [Trans]  +  sum_v R_v  [gravity term per row]
+         + 7 Nc  [P, accum_prev, porosity, Sr, alpha, m, volume]
+         + N_bD  [Dirichlet boundary pressures]  + Nc  [R out]  + nnz  [J out])."""
+    nbd = int(np.sum(view["bnd_has_value"] * (view["bnd_type"] != 1)))
+    return 8 * (int(view["ntrans_total"]) + int(view["nrows_total"]) + 7 * view["ncells"] + nbd + view["ncells"]
+                + int(view["nnz"]))
+
+
+def vertex_kernel_bytes(view):
+    """Algorithmic bytes of one vertex_kernel launch: its Trans blocks, one
+    gravity coefficient per row, one read of the per-cell/per-boundary state it
+    upwinds on (P, rho, drho, lam, dlam) and its per-vertex partial outputs."""
+    nint = view["v_nint"].astype(np.int64)
+    partials = int(np.sum(nint * nint + nint))
+    nb = view["nbnd"]
+    return 8 * (int(view["ntrans_total"]) + int(view["nrows_total"]) + 5 * (view["ncells"] + nb) + partials)
+
+
+def fp64_flops_per_eval(view):
+    """FP64 operations of one evaluation by the vertex/cell decomposition:
+    2 per Trans entry (T.P), 2 per (row, internal column, adjacent cell) for J,
+    ~24 per row for upwinding and the flux/derivative scalars, and one add per
+    gathered partial."""
+    v_rows = np.diff(view["v_row_off"]).astype(np.int64)
+    nint = view["v_nint"].astype(np.int64)
+    tp = 2 * int(view["ntrans_total"])
+    jac = int(np.sum(v_rows * nint)) * 4
+    rows = 24 * int(view["nrows_total"])
+    gather = int(np.sum(nint * nint + nint))
+    return tp + jac + rows + gather
+
+
+def cpu_baseline(view, U, Uprev, budget_s=12.0, threads=None):
+    """Oracle F+J (reference loop order, colour-parallel) on the host cores."""
+    from oracle import Oracle
+
+    cores = threads or len(os.sched_getaffinity(0))
+    t0 = time.perf_counter()
+    o = Oracle(view)
+    o.snes_presolve(Uprev, DT)
+    log(f"oracle ready in {time.perf_counter() - t0:.1f} s; timing on {cores} threads")
+    o.snes_function_jacobian_parallel(U, cores)  # warm-up
+    n, t0 = 0, time.perf_counter()
+    while True:
+        o.snes_function_jacobian_parallel(U, cores)
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= budget_s or n >= 50:
+            break
+    return view["ncells"] * n / el, cores, n, el
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    t, U, Uprev, info = build_workload(host_only=True)
+    view = t.setup_view()
+    from oracle import Oracle
+
+    cores = len(os.sched_getaffinity(0))
+    o = Oracle(view)
+    o.snes_presolve(Uprev, DT)
+    for _ in range(max(1, min(args.warmup, 3))):
+        o.snes_function_jacobian_parallel(U, cores)
+    steps = max(1, min(args.steps, 20))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        o.snes_function_jacobian_parallel(U, cores)
+    el = time.perf_counter() - t0
+    value = view["ncells"] * steps / el
+    out = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": info["workload"], "ncells": view["ncells"], "form": "SNES F+J",
+                   "l2": "inputs larger than L2"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{steps} full F+J evaluations of the {view['ncells']}-cell workload"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "C restatement of the reference loops (oracle/); the reference needs PETSc+MPI, absent here",
+    }
+    print(json.dumps(out), flush=True)
+
+
+def run_gpu(args, rank, world, local_rank):
+    import torch
+
+    import tdycore_gb300 as T
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    t, U, Uprev, info = build_workload()
+    view = t.setup_view()
+    nc, nnz = t.ncells, t.nnz
+    t.set_dtime(DT)
+    dev = torch.device("cuda", local_rank)
+    stream = torch.cuda.Stream(device=dev)
+    dU = torch.tensor(U, dtype=torch.float64, device=dev)
+    dUp = torch.tensor(Uprev, dtype=torch.float64, device=dev)
+    dR = torch.empty(nc, dtype=torch.float64, device=dev)
+    dJ = torch.empty(nnz, dtype=torch.float64, device=dev)
+    sp = stream.cuda_stream
+    t.presolve_device(dUp, stream=sp)
+    for _ in range(args.warmup):
+        t.snes_function_jacobian_device(dU, dR, dJ, stream=sp)
+    torch.cuda.synchronize(dev)
+
+    # device-resident throughput
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    with ClockSampler(local_rank) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            t.snes_function_jacobian_device(dU, dR, dJ, stream=sp)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        if args.steps * 0.001 < 1.0:  # keep sampling ~1 s of load for the clock record
+            tt = time.perf_counter()
+            while time.perf_counter() - tt < 1.0:
+                t.snes_function_jacobian_device(dU, dR, dJ, stream=sp)
+                torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1)
+    if dist:
+        tms = torch.tensor([ms], device=dev)
+        dist.all_reduce(tms, op=dist.ReduceOp.MAX)
+        ms = float(tms.item())
+    ms_per_step = ms / args.steps
+    value = world * nc * args.steps / (ms * 1e-3)
+
+    # per-kernel durations (events between launches)
+    t.set_timers(True)
+    kt_steps = min(args.steps, 50)
+    for _ in range(kt_steps):
+        t.snes_function_jacobian_device(dU, dR, dJ, stream=sp)
+    timers = t.timers()
+    t.set_timers(False)
+    kernel_ms = {k: v[0] / max(v[1], 1) for k, v in timers.items()}
+    eval_ms = sum(kernel_ms.values())
+
+    # end to end through the host-pointer C-ABI (pinned buffers)
+    Uh = torch.tensor(U, dtype=torch.float64).pin_memory()
+    Rh = torch.empty(nc, dtype=torch.float64).pin_memory()
+    Jh = torch.empty(nnz, dtype=torch.float64).pin_memory()
+    Un, Rn, Jn = Uh.numpy(), Rh.numpy(), Jh.numpy()
+    t.presolve(Uprev)
+    for _ in range(2):
+        t.snes_function_jacobian(Un, Rn, Jn)
+    e2e_steps = max(3, min(args.steps, 30))
+    if dist:
+        dist.barrier()
+    tt = time.perf_counter()
+    for _ in range(e2e_steps):
+        t.snes_function_jacobian(Un, Rn, Jn)
+    e2e_s = time.perf_counter() - tt
+    if dist:
+        te = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(te, op=dist.ReduceOp.MAX)
+        e2e_s = float(te.item())
+    e2e_value = world * nc * e2e_steps / e2e_s
+
+    if rank == 0:
+        hbm_peak, peak_kind = peaks()
+        try:
+            fp64_peak = T.device_fp64_tflops()
+        except Exception:
+            fp64_peak = None
+        vb = vertex_kernel_bytes(view)
+        vk_ms = kernel_ms.get("vertex_kernel", float("nan"))
+        achieved = vb / (vk_ms * 1e-3) / 1e9
+        balg = algorithmic_bytes(view)
+        flops = fp64_flops_per_eval(view)
+        traffic = None
+        tf = ROOT / "profiles" / "vertex_kernel_traffic.json"
+        if tf.exists():
+            try:
+                traffic = json.loads(tf.read_text()).get("bytes_per_launch_full_workload")
+            except Exception:
+                traffic = None
+        cpu_v, cores, n_cpu, cpu_s = cpu_baseline(view, U, Uprev, budget_s=args.cpu_budget)
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": info["workload"], "ncells": nc, "nnz_jacobian": nnz, "form": "SNES F+J",
+                       "seed": info["seed"], "l2": "inputs larger than L2 (no flush)",
+                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+            "roofline": {"bound": "hbm", "kernel": "vertex_kernel", "achieved": achieved, "peak": hbm_peak,
+                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm_peak,
+                         "traffic": traffic, "algorithmic_bytes_per_launch": vb,
+                         "avg_launch_ms": vk_ms},
+            "roofline_evaluation": {"algorithmic_bytes": balg, "GBps": balg / (ms_per_step * 1e-3) / 1e9,
+                                    "frac_hbm": balg / (ms_per_step * 1e-3) / 1e9 / hbm_peak,
+                                    "bytes_per_cell": balg / nc},
+            "fp64": {"flops_per_eval": flops, "achieved_tflops": flops / (ms_per_step * 1e-3) / 1e12,
+                     "peak_tflops_probe": fp64_peak,
+                     "frac": (flops / (ms_per_step * 1e-3) / 1e12 / fp64_peak) if fp64_peak else None},
+            "kernel_ms": kernel_ms,
+            "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{n_cpu} full F+J evaluations ({cpu_s:.1f} s) of the same workload"},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * nc,
+                    "d2h_bytes_per_step": 8 * (nc + nnz), "steps": e2e_steps},
+            "gpu_launches": args.steps * t.launches_per_evaluation(),
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(out), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-budget", type=float, default=12.0)
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank)
+    else:
+        run_gpu(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    main()

@@ -189,6 +189,18 @@ TDyErrorCode TDyPreSolveSNESSolverDevice(TDy tdy, const double *dU_prev, void *s
 TDyErrorCode TDyGetLaunchesPerEvaluation(TDy tdy, int *nlaunch);
 TDyErrorCode TDySynchronize(TDy tdy);
 
+/* Per-kernel timers, the analogue of the reference's TDY_START_FUNCTION_TIMER
+ * event log (include/tdytimers.h; -tdy_timers).  While enabled every
+ * evaluation records CUDA events between its kernels and waits for them, so
+ * enable timers for measurement runs only.  TDyGetTimers fills up to *n
+ * entries (kernel name, total milliseconds, launch count) and sets *n to the
+ * number of timed kernels. */
+TDyErrorCode TDySetTimersEnabled(TDy tdy, int on);
+TDyErrorCode TDyGetTimers(TDy tdy, int *n, const char **names, double *ms_total, long long *calls);
+/* Achieved FP64 FMA throughput of the current device (TFLOP/s), the
+ * denominator of the FP64 roofline fraction reported beside HBM. */
+TDyErrorCode TDyDeviceFP64Throughput(double *tflops);
+
 /* State and diagnostics: TDyUpdateState (src/tdycore.c:1461) and
  * TDyGetLiquidSaturation/TDyGetLiquidMass (include/tdycore.h:213-215).
  * Outputs are host arrays of ncells values. */

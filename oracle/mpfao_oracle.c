@@ -36,8 +36,8 @@ struct OracleCtx {
   double *S, *dS_dP, *d2S_dP2, *Kr, *dKr_dS, *rho, *drho_dP, *d2rho_dP2, *vis, *dvis_dP;
   /* boundary state */
   double *P_bnd, *S_bnd, *Kr_bnd, *dKr_dS_bnd;
-  /* P_vec, TtimesP_vec */
-  double *P_vec, *TtimesP;
+  /* P_vec, TtimesP_vec, and sum_c |T_rc P_c| (error scale of each row) */
+  double *P_vec, *TtimesP, *TPabs;
   /* Trans_mat as CSR over vertex rows, columns ascending */
   int *tm_rowptr, *tm_col;
   double *tm_val;
@@ -273,6 +273,7 @@ OracleCtx *oracle_create(const OracleInput *in) {
   ALLOC(c->dKr_dS_bnd, nb);
   ALLOC(c->P_vec, nc + nb);
   ALLOC(c->TtimesP, nrows);
+  ALLOC(c->TPabs, nrows);
   ALLOC(c->accum_prev, nc);
 #undef ALLOC
 
@@ -403,7 +404,7 @@ OracleCtx *oracle_create(const OracleInput *in) {
 void oracle_destroy(OracleCtx *c) {
   if (!c) return;
   double *arr[] = {c->S, c->dS_dP, c->d2S_dP2, c->Kr, c->dKr_dS, c->rho, c->drho_dP, c->d2rho_dP2, c->vis,
-                   c->dvis_dP, c->P_bnd, c->S_bnd, c->Kr_bnd, c->dKr_dS_bnd, c->P_vec, c->TtimesP, c->accum_prev,
+                   c->dvis_dP, c->P_bnd, c->S_bnd, c->Kr_bnd, c->dKr_dS_bnd, c->P_vec, c->TtimesP, c->TPabs, c->accum_prev,
                    c->tm_val};
   for (size_t i = 0; i < sizeof(arr) / sizeof(arr[0]); i++) free(arr[i]);
   free(c->tm_rowptr);
@@ -486,9 +487,13 @@ static void update_boundary_range(OracleCtx *c, const double *U, int lo, int hi)
 /* MatMult(Trans_mat, P_vec, TtimesP_vec) (tdympfao_ts.c:184) */
 static void matmult_range(OracleCtx *c, int lo, int hi) {
   for (int r = lo; r < hi; r++) {
-    double s = 0.0;
-    for (int k = c->tm_rowptr[r]; k < c->tm_rowptr[r + 1]; k++) s += c->tm_val[k] * c->P_vec[c->tm_col[k]];
+    double s = 0.0, a = 0.0;
+    for (int k = c->tm_rowptr[r]; k < c->tm_rowptr[r + 1]; k++) {
+      s += c->tm_val[k] * c->P_vec[c->tm_col[k]];
+      a += fabs(c->tm_val[k] * c->P_vec[c->tm_col[k]]);
+    }
     c->TtimesP[r] = s;
+    c->TPabs[r] = a;
   }
 }
 
@@ -543,13 +548,15 @@ static void ifunction_vertex(OracleCtx *c, int v, double *r, double *rmag) {
       fluxm = den_aveg * ukvr * (-TtimesP);
       fluxm += -pow(den_aveg, 2.0) * ukvr * G;
     }
+    /* error scale of fluxm: |rho ukvr| (sum_c |T_c P_c| + |rho G|) */
+    double fmag = set_flow_to_zero ? 0.0 : fabs(den_aveg * ukvr) * (c->TPabs[r0 + irow] + fabs(den_aveg * G));
     if (cell_id_up >= 0) {
       r[cell_id_up] += fluxm;
-      if (rmag) rmag[cell_id_up] += fabs(fluxm);
+      if (rmag) rmag[cell_id_up] += fmag;
     }
     if (cell_id_dn >= 0) {
       r[cell_id_dn] -= fluxm;
-      if (rmag) rmag[cell_id_dn] += fabs(fluxm);
+      if (rmag) rmag[cell_id_dn] += fmag;
     }
   }
 }
@@ -604,7 +611,7 @@ void oracle_ts_ifunction(OracleCtx *c, const double *U, const double *Ut, double
 
 /* MatSetValuesLocal(A, 1, &row, n, cols, vals, ADD_VALUES) */
 static inline void mat_add_row(OracleCtx *c, double *J, double *Jmag, int row, int n, const int *cols,
-                               const double *vals) {
+                               const double *vals, const double *mags) {
   const int *rc = c->colidx + c->rowptr[row];
   int rn = c->rowptr[row + 1] - c->rowptr[row];
   for (int j = 0; j < n; j++) {
@@ -623,7 +630,7 @@ static inline void mat_add_row(OracleCtx *c, double *J, double *Jmag, int row, i
     }
     if (pos < 0) abort(); /* column outside the preallocated pattern */
     J[c->rowptr[row] + pos] += vals[j];
-    if (Jmag) Jmag[c->rowptr[row] + pos] += fabs(vals[j]);
+    if (Jmag) Jmag[c->rowptr[row] + pos] += mags ? mags[j] : fabs(vals[j]);
   }
 }
 
@@ -635,7 +642,7 @@ static void ijacobian_vertex(OracleCtx *c, int v, double *J, double *Jmag) {
   int num_int_cells = in->v_nint[v];
   const double *Tv = in->trans + in->v_trans_off[v];
   int up_cols[256], dn_cols[256];
-  double up_Jac[256], dn_Jac[256];
+  double up_Jac[256], dn_Jac[256], mag[256];
   for (int irow = 0; irow < nr; irow++) {
     int set_jac_to_zero = 0;
     int face_id = in->row_face[r0 + irow];
@@ -694,16 +701,23 @@ static void ijacobian_vertex(OracleCtx *c, int v, double *J, double *Jmag) {
       int cell_id = in->col_ext[c0 + icol];
       double T = Tv[(long long)irow * ncl + icol];
       double Jac;
+      const double tpa = c->TPabs[r0 + irow];
       if (set_jac_to_zero) {
         Jac = 0.0;
+        mag[icol] = 0.0;
       } else if (cell_id_up > -1 && cell_id == cell_id_up) {
         Jac = dden_aveg_dPup * ukvr * TtimesP + den_aveg * dukvr_dPup * TtimesP + den_aveg * ukvr * T +
               2 * den_aveg * dden_aveg_dPup * ukvr * G + pow(den_aveg, 2.0) * dukvr_dPup * G;
+        mag[icol] = fabs(dden_aveg_dPup * ukvr) * tpa + fabs(den_aveg * dukvr_dPup) * tpa + fabs(den_aveg * ukvr * T) +
+                    fabs(2 * den_aveg * dden_aveg_dPup * ukvr * G) + fabs(pow(den_aveg, 2.0) * dukvr_dPup * G);
       } else if (cell_id_dn > -1 && cell_id == cell_id_dn) {
         Jac = dden_aveg_dPdn * ukvr * TtimesP + den_aveg * dukvr_dPdn * TtimesP + den_aveg * ukvr * T +
               2 * den_aveg * dden_aveg_dPdn * ukvr * G + pow(den_aveg, 2.0) * dukvr_dPdn * G;
+        mag[icol] = fabs(dden_aveg_dPdn * ukvr) * tpa + fabs(den_aveg * dukvr_dPdn) * tpa + fabs(den_aveg * ukvr * T) +
+                    fabs(2 * den_aveg * dden_aveg_dPdn * ukvr * G) + fabs(pow(den_aveg, 2.0) * dukvr_dPdn * G);
       } else {
         Jac = den_aveg * ukvr * T;
+        mag[icol] = fabs(Jac);
       }
       Jac = -Jac;
       if (cell_id_up >= 0) {
@@ -715,8 +729,8 @@ static void ijacobian_vertex(OracleCtx *c, int v, double *J, double *Jmag) {
         dn_Jac[icol] = -Jac;
       }
     }
-    if (cell_id_up >= 0) mat_add_row(c, J, Jmag, cell_id_up, num_int_cells, up_cols, up_Jac);
-    if (cell_id_dn >= 0) mat_add_row(c, J, Jmag, cell_id_dn, num_int_cells, dn_cols, dn_Jac);
+    if (cell_id_up >= 0) mat_add_row(c, J, Jmag, cell_id_up, num_int_cells, up_cols, up_Jac, mag);
+    if (cell_id_dn >= 0) mat_add_row(c, J, Jmag, cell_id_dn, num_int_cells, dn_cols, dn_Jac, mag);
   }
 }
 
@@ -735,7 +749,7 @@ void oracle_snes_jacobian(OracleCtx *c, const double *U, double *J, double *Jmag
     double dmass_dP = c->rho[i] * dporosity_dP * c->S[i] + c->drho_dP[i] * in->porosity[i] * c->S[i] +
                       c->rho[i] * in->porosity[i] * c->dS_dP[i];
     double Jac = dmass_dP * in->volume[i] * dtInv;
-    mat_add_row(c, J, Jmag, i, 1, &i, &Jac);
+    mat_add_row(c, J, Jmag, i, 1, &i, &Jac, NULL);
   }
 }
 
@@ -757,7 +771,7 @@ void oracle_ts_ijacobian(OracleCtx *c, const double *U, const double *Ut, double
                          dS * drho_dP * poro + S * d2rho_dP2 * poro + S * drho_dP * dporosity_dP +
                          d2S * rho * poro + dS * drho_dP * poro + dS * rho * dporosity_dP);
     double value = (shift * dmass_dP + d2mass_dP2 * Ut[icell]) * in->volume[icell];
-    mat_add_row(c, J, Jmag, icell, 1, &icell, &value);
+    mat_add_row(c, J, Jmag, icell, 1, &icell, &value, NULL);
   }
 }
 
@@ -799,7 +813,7 @@ void oracle_snes_function_jacobian_parallel(OracleCtx *c, const double *U, doubl
       double dmass_dP = c->rho[i] * 0.0 * c->S[i] + c->drho_dP[i] * in->porosity[i] * c->S[i] +
                         c->rho[i] * in->porosity[i] * c->dS_dP[i];
       double Jac = dmass_dP * in->volume[i] * dtInv;
-      mat_add_row(c, J, NULL, i, 1, &i, &Jac);
+      mat_add_row(c, J, NULL, i, 1, &i, &Jac, NULL);
     }
   }
 }

@@ -58,7 +58,10 @@ void oracle_pattern(OracleCtx *ctx, int *rowptr, int *colidx);
 /* TDyMPFAOSNESPreSolve (tdympfao_snes.c:32-64) */
 void oracle_snes_presolve(OracleCtx *ctx, const double *Uprev, double dt);
 /* TDyMPFAOSNESFunction (tdympfao_snes.c:67-140); Rmag (may be NULL) receives
- * the sum of absolute values of every term added into R[i]. */
+ * the floating-point error scale of R[i]: for each flux added into R[i],
+ * |rho ukvr| (sum_c |T_c P_c| + |rho G|), plus the absolute accumulation
+ * terms.  Jmag likewise holds, per entry, the sum of the error scales of the
+ * contributions (products evaluated in absolute value). */
 void oracle_snes_function(OracleCtx *ctx, const double *U, double *R, double *Rmag);
 /* TDyMPFAOSNESJacobian (tdympfao_snes.c:143-203); J in pattern order. */
 void oracle_snes_jacobian(OracleCtx *ctx, const double *U, double *J, double *Jmag);

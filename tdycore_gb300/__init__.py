@@ -134,6 +134,16 @@ _sig("TDyUpdateState", c_void_p, _dp, c_int)
 _sig("TDyGetLiquidSaturation", c_void_p, _dp)
 _sig("TDyGetLiquidMass", c_void_p, _dp)
 _sig("TDyMPFAOGetSetupView", c_void_p, POINTER(TDyMPFAOSetupView))
+_sig("TDySetTimersEnabled", c_void_p, c_int)
+_sig("TDyGetTimers", c_void_p, _ip, POINTER(c_char_p), _dp, POINTER(c_longlong))
+_sig("TDyDeviceFP64Throughput", _dp)
+
+
+def device_fp64_tflops() -> float:
+    """Measured FP64 FMA throughput of the current CUDA device."""
+    x = c_double()
+    check(lib.TDyDeviceFP64Throughput(byref(x)), "TDyDeviceFP64Throughput")
+    return x.value
 
 
 class TDyError(RuntimeError):
@@ -423,10 +433,15 @@ class TDy:
         check(lib.TDyMPFAOSNESJacobian(self._h, _as_dp(u), _as_dp(J)), "TDyMPFAOSNESJacobian")
         return J
 
-    def snes_function_jacobian(self, U):
+    def snes_function_jacobian(self, U, R=None, J=None):
+        """Fused residual + Jacobian; R and J may be caller-owned (e.g. pinned) float64 arrays."""
         u = _f64(U, self.ncells)
-        R = np.empty(self.ncells)
-        J = np.empty(self.nnz)
+        R = np.empty(self.ncells) if R is None else R
+        J = np.empty(self.nnz) if J is None else J
+        if R.dtype != np.float64 or J.dtype != np.float64 or not (R.flags.c_contiguous and J.flags.c_contiguous):
+            raise ValueError("R and J must be contiguous float64 arrays")
+        if R.size != self.ncells or J.size != self.nnz:
+            raise ValueError("R or J has the wrong size")
         check(lib.TDyMPFAOSNESFunctionJacobian(self._h, _as_dp(u), _as_dp(R), _as_dp(J)),
               "TDyMPFAOSNESFunctionJacobian")
         return R, J
@@ -484,6 +499,18 @@ class TDy:
 
     def synchronize(self):
         check(lib.TDySynchronize(self._h), "TDySynchronize")
+
+    # timers -----------------------------------------------------------------
+    def set_timers(self, on: bool):
+        check(lib.TDySetTimersEnabled(self._h, 1 if on else 0), "TDySetTimersEnabled")
+
+    def timers(self) -> dict:
+        n = c_int(8)
+        names = (c_char_p * 8)()
+        ms = (c_double * 8)()
+        calls = (c_longlong * 8)()
+        check(lib.TDyGetTimers(self._h, byref(n), names, ms, calls), "TDyGetTimers")
+        return {names[i].decode(): (ms[i], calls[i]) for i in range(n.value)}
 
     # diagnostics ------------------------------------------------------------
     def update_state(self, U):

@@ -920,4 +920,20 @@ TDyErrorCode TDyGetLiquidMass(TDy tdy, double *mass) {
   return device_get_diagnostic(tdy, 1, mass);
 }
 
+TDyErrorCode TDySetTimersEnabled(TDy tdy, int on) {
+  TDY_CHECK_HANDLE(tdy);
+  TDY_CHECK_DEVICE(tdy);
+  return device_set_timers(tdy, on);
+}
+TDyErrorCode TDyGetTimers(TDy tdy, int *n, const char **names, double *ms_total, long long *calls) {
+  TDY_CHECK_HANDLE(tdy);
+  TDY_CHECK_DEVICE(tdy);
+  if (!n) return set_error(TDY_ERR_ARG_NULL, "null count");
+  return device_get_timers(tdy, n, names, ms_total, calls);
+}
+TDyErrorCode TDyDeviceFP64Throughput(double *tflops) {
+  if (!tflops) return set_error(TDY_ERR_ARG_NULL, "null output");
+  return device_fp64_probe(tflops);
+}
+
 }  // extern "C"

@@ -20,5 +20,8 @@ int device_launches_per_eval(_p_TDy *t);
 int device_synchronize(_p_TDy *t);
 int device_update_state_host(_p_TDy *t, const double *U);
 int device_get_diagnostic(_p_TDy *t, int which, double *out);
+int device_set_timers(_p_TDy *t, int on);
+int device_get_timers(_p_TDy *t, int *n, const char **names, double *ms, long long *calls);
+int device_fp64_probe(double *tflops);
 
 }  // namespace tdy

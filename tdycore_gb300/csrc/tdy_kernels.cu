@@ -71,9 +71,16 @@ struct DevArgs {
   double *R, *J;
 };
 
+static const char *const kKernelNames[3] = {"state_kernel", "vertex_kernel", "cell_kernel"};
+
 struct DeviceState {
   cudaStream_t stream = nullptr;
   DevArgs a;
+  // per-kernel timers (TDY_START_FUNCTION_TIMER analogue, include/tdytimers.h)
+  bool timers = false;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  double t_ms[3] = {0, 0, 0};
+  long long t_calls[3] = {0, 0, 0};
   // owned allocations
   std::vector<void *> allocs;
   double *dU = nullptr, *dUt = nullptr, *dR = nullptr, *dJ = nullptr;
@@ -532,6 +539,8 @@ void device_destroy(_p_TDy *t) {
   DeviceState *d = t->dev;
   if (!d) return;
   if (d->stream) cudaStreamSynchronize(d->stream);
+  for (int k = 0; k < 4; k++)
+    if (d->ev[k]) cudaEventDestroy(d->ev[k]);
   for (void *p : d->allocs) cudaFree(p);
   if (d->stream) cudaStreamDestroy(d->stream);
   delete d;
@@ -582,10 +591,93 @@ int device_eval(_p_TDy *t, int form, double time, const double *dU, const double
   a.needJ = dJ != nullptr;
   a.R = dR;
   a.J = dJ;
+  if (d->timers) CUDA_TRY(cudaEventRecord(d->ev[0], st));
   state_kernel<<<nblocks(a.nc + a.nb, 256), 256, 0, st>>>(a);
+  if (d->timers) CUDA_TRY(cudaEventRecord(d->ev[1], st));
   vertex_kernel<<<nblocks(a.nv, 128), 128, 0, st>>>(a);
+  if (d->timers) CUDA_TRY(cudaEventRecord(d->ev[2], st));
   cell_kernel<<<nblocks(a.nc, 128), 128, 0, st>>>(a);
+  if (d->timers) CUDA_TRY(cudaEventRecord(d->ev[3], st));
   CUDA_TRY(cudaGetLastError());
+  if (d->timers) {
+    CUDA_TRY(cudaEventSynchronize(d->ev[3]));
+    for (int k = 0; k < 3; k++) {
+      float ms = 0.f;
+      CUDA_TRY(cudaEventElapsedTime(&ms, d->ev[k], d->ev[k + 1]));
+      d->t_ms[k] += ms;
+      d->t_calls[k] += 1;
+    }
+  }
+  return 0;
+}
+
+int device_set_timers(_p_TDy *t, int on) {
+  DeviceState *d = t->dev;
+  if (on && !d->ev[0])
+    for (int k = 0; k < 4; k++) CUDA_TRY(cudaEventCreate(&d->ev[k]));
+  d->timers = on != 0;
+  for (int k = 0; k < 3; k++) {
+    d->t_ms[k] = 0.0;
+    d->t_calls[k] = 0;
+  }
+  return 0;
+}
+
+int device_get_timers(_p_TDy *t, int *n, const char **names, double *ms, long long *calls) {
+  DeviceState *d = t->dev;
+  int cap = *n;
+  *n = 3;
+  for (int k = 0; k < 3 && k < cap; k++) {
+    if (names) names[k] = kKernelNames[k];
+    if (ms) ms[k] = d->t_ms[k];
+    if (calls) calls[k] = d->t_calls[k];
+  }
+  return 0;
+}
+
+// FP64 throughput probe: independent FMA chains per thread, enough blocks to
+// fill every SM; reports achieved double-precision TFLOP/s on the device.
+__global__ void __launch_bounds__(256) fp64_probe_kernel(double *out, int iters) {
+  double a0 = threadIdx.x * 1e-9, a1 = a0 + 1e-9, a2 = a0 + 2e-9, a3 = a0 + 3e-9;
+  double a4 = a0 + 4e-9, a5 = a0 + 5e-9, a6 = a0 + 6e-9, a7 = a0 + 7e-9;
+  const double b = 0.999999999, c = 1e-12;
+  for (int i = 0; i < iters; i++) {
+    a0 = fma(a0, b, c);
+    a1 = fma(a1, b, c);
+    a2 = fma(a2, b, c);
+    a3 = fma(a3, b, c);
+    a4 = fma(a4, b, c);
+    a5 = fma(a5, b, c);
+    a6 = fma(a6, b, c);
+    a7 = fma(a7, b, c);
+  }
+  double s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+  if (s == 12345.678) out[blockIdx.x] = s;  // keep the chains live
+}
+
+int device_fp64_probe(double *tflops) {
+  int dev = 0, nsm = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  double *out = nullptr;
+  CUDA_TRY(cudaMalloc(&out, sizeof(double) * nsm * 8));
+  cudaEvent_t e0, e1;
+  CUDA_TRY(cudaEventCreate(&e0));
+  CUDA_TRY(cudaEventCreate(&e1));
+  const int iters = 4096, blocks = nsm * 8, threads = 256;
+  fp64_probe_kernel<<<blocks, threads>>>(out, iters);  // warm-up
+  CUDA_TRY(cudaEventRecord(e0));
+  const int reps = 5;
+  for (int r = 0; r < reps; r++) fp64_probe_kernel<<<blocks, threads>>>(out, iters);
+  CUDA_TRY(cudaEventRecord(e1));
+  CUDA_TRY(cudaEventSynchronize(e1));
+  float ms = 0.f;
+  CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  double flops = 2.0 * 8.0 * iters * (double)blocks * threads * reps;
+  *tflops = flops / (ms * 1e-3) / 1e12;
   return 0;
 }
 

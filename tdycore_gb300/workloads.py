@@ -1,0 +1,213 @@
+"""Seeded synthetic workloads for the MPFA-O Richards path.
+
+Each builder returns a configured (not yet set up) :class:`tdycore_gb300.TDy`
+together with the pressure state to evaluate.  Fields are drawn from seeded
+generators so every run, test and benchmark sees the same inputs.
+
+* ``box_column``      -- the reference's regression geometries
+  (demo/transient/transient_snes_mpfaof90.F90, transient_mpfaof90.F90).
+* ``hydrostatic_box`` -- 10x10x10 cells over a 1 m cube, k = 1e-11 m^2,
+  porosity 0.25, van Genuchten alpha = 1e-4 Pa^-1, m = 0.3, Sr = 0.15,
+  hydrostatic pressure with 101325 Pa at the top face, rho = 998.2 kg/m^3
+  (the density constant of this workload; the reference's constant-density
+  EOS uses 998.0), Dirichlet on the top face and no flow elsewhere.
+* ``spe10_like``      -- 60x220x85 hexahedra over 365.76 x 670.56 x 51.816 m
+  (the SPE10 model-2 grid) with vertices jittered by up to 10% of the cell
+  size (x, y per vertical vertex line, z per vertex), log10 k ~ N(-13, 1.5^2)
+  smoothed by a 5-cell Gaussian kernel and re-standardised, kz = 0.1 kh,
+  porosity ~ U(0.05, 0.35), alpha ~ logU(1e-5, 1e-3), m ~ U(0.2, 0.6) per
+  cell, and hydrostatic pressure plus N(0, 5e3 Pa) noise.  A seeded
+  synthetic field stands in for the SPE10 permeability data.
+* ``wedge_extruded``  -- a seeded Delaunay triangulation extruded into
+  layers (prisms), full-tensor permeability with random rotations.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import (DIRICHLET_BC, NEUMANN_BC, WATER_DENSITY_CONSTANT, WATER_DENSITY_EXPONENTIAL, TDy,
+               create_richards_mpfao)
+
+MASTER_SEED = 20261203
+GRAVITY = 9.8068
+PREF = 101325.0
+
+
+def _rng(sub: int) -> np.random.Generator:
+    return np.random.default_rng([MASTER_SEED, sub])
+
+
+def structured_surface(nx, ny, lx, ly, jitter=0.0, rng=None):
+    """Surface vertices (x fastest) and counter-clockwise quads of an nx*ny grid."""
+    xs = np.linspace(0.0, lx, nx + 1)
+    ys = np.linspace(0.0, ly, ny + 1)
+    X, Y = np.meshgrid(xs, ys, indexing="xy")
+    if jitter > 0.0:
+        dx, dy = lx / nx, ly / ny
+        jx = rng.uniform(-jitter, jitter, X.shape) * dx
+        jy = rng.uniform(-jitter, jitter, Y.shape) * dy
+        jx[:, 0] = jx[:, -1] = 0.0
+        jy[0, :] = jy[-1, :] = 0.0
+        X = X + jx
+        Y = Y + jy
+    xy = np.stack([X.ravel(), Y.ravel()], axis=1)
+    j, i = np.meshgrid(np.arange(ny), np.arange(nx), indexing="ij")
+    v0 = (j * (nx + 1) + i).ravel()
+    quads = np.stack([v0, v0 + 1, v0 + nx + 2, v0 + nx + 1], axis=1).astype(np.int32)
+    return xy, quads
+
+
+def layered_z(nv2, nz, lz, jitter=0.0, rng=None, ztop=None):
+    """Vertex elevations per level (level-major), optional per-vertex jitter."""
+    levels = np.linspace(0.0, lz, nz + 1)
+    z = np.repeat(levels[:, None], nv2, axis=1)
+    if jitter > 0.0:
+        dz = lz / nz
+        jz = rng.uniform(-jitter, jitter, z.shape) * dz
+        jz[0, :] = jz[-1, :] = 0.0
+        z = z + jz
+    return z
+
+
+def hydrostatic(zc, ztop, rho, g=GRAVITY, ptop=PREF):
+    return ptop + rho * g * (ztop - zc)
+
+
+def box_column(nx, ny, nz, *, density=WATER_DENSITY_EXPONENTIAL, gmatrix=0, bc_type=None, pfunc=None,
+               perm=1e-10, porosity=0.115, sr=0.115) -> TDy:
+    """The reference's transient regression geometry on [0,1]^3."""
+    t = create_richards_mpfao()
+    t.set_box_mesh(nx, ny, nz)
+    t.set_from_options()
+    t.set_constant_tensor_permeability([perm, 0, 0, 0, perm, 0, 0, 0, perm])
+    t.set_constant_residual_saturation(sr)
+    t.set_constant_porosity(porosity)
+    t.set_water_density_type(density)
+    t.set_gmatrix_method(gmatrix)
+    if bc_type is not None:
+        t.set_boundary_condition_type(bc_type)
+    if pfunc is not None:
+        t.set_boundary_pressure_function(pfunc)
+    return t
+
+
+def top_dirichlet_types(ztop, tol=1e-9):
+    return lambda x, y, z: DIRICHLET_BC if z > ztop - tol else NEUMANN_BC
+
+
+def hydrostatic_box(n=10, rho=998.2):
+    """10x10x10 box workload; returns (tdy, U0, info)."""
+    t = create_richards_mpfao()
+    t.set_box_mesh(n, n, n)
+    t.set_from_options()
+    t.set_constant_isotropic_permeability(1e-11)
+    t.set_constant_porosity(0.25)
+    t.set_constant_residual_saturation(0.15)
+    nc = n ** 3
+    t.set_vangenuchten_values(np.full(nc, 0.3), np.full(nc, 1e-4))
+    t.set_mualem_values(np.full(nc, 0.3))
+    t.set_water_density_type(WATER_DENSITY_CONSTANT)
+    t.set_boundary_pressure_type_function(top_dirichlet_types(1.0))
+    t.set_boundary_pressure_function(lambda x, y, z: PREF)
+    k = np.arange(nc) // (n * n)
+    zc = (k + 0.5) / n
+    U0 = hydrostatic(zc, 1.0, rho)
+    return t, U0, {"workload": f"hydrostatic_box_{n}x{n}x{n}", "ncells": nc, "rho": rho}
+
+
+def _correlated_log10k(shape, rng, mean=-13.0, std=1.5, sigma=5.0):
+    from scipy.ndimage import gaussian_filter
+
+    g = rng.standard_normal(shape)
+    g = gaussian_filter(g, sigma=sigma, mode="reflect")
+    g = (g - g.mean()) / g.std()
+    return mean + std * g
+
+
+def spe10_like(nx=60, ny=220, nz=85, lx=365.76, ly=670.56, lz=51.816, jitter=0.10, seed_offset=0):
+    """The 60x220x85 jittered hex workload; returns (tdy, U, info)."""
+    rng = _rng(1 + seed_offset)
+    xy, quads = structured_surface(nx, ny, lx, ly, jitter, rng)
+    z = layered_z(xy.shape[0], nz, lz, jitter, _rng(2 + seed_offset))
+    t = create_richards_mpfao()
+    t.set_extruded_mesh(xy, quads, z)
+    t.set_from_options()
+    nc = nx * ny * nz
+    log10k = _correlated_log10k((nz, ny, nx), _rng(3 + seed_offset)).ravel()
+    kh = 10.0 ** log10k
+    K = np.zeros((nc, 9))
+    K[:, 0] = kh
+    K[:, 4] = kh
+    K[:, 8] = 0.1 * kh
+    t.set_permeability_values(K)
+    r = _rng(4 + seed_offset)
+    t.set_porosity_values(r.uniform(0.05, 0.35, nc))
+    alpha = 10.0 ** r.uniform(-5.0, -3.0, nc)
+    m = r.uniform(0.2, 0.6, nc)
+    t.set_vangenuchten_values(m, alpha)
+    t.set_mualem_values(m)
+    t.set_constant_residual_saturation(0.15)
+    t.set_water_density_type(WATER_DENSITY_CONSTANT)
+    t.set_boundary_pressure_type_function(top_dirichlet_types(lz))
+    t.set_boundary_pressure_function(lambda x, y, zz: PREF)
+    # cell-centre elevations: mean of the 8 vertex elevations
+    zl = z.reshape(nz + 1, ny + 1, nx + 1)
+    zc = 0.125 * (zl[:-1, :-1, :-1] + zl[:-1, :-1, 1:] + zl[:-1, 1:, :-1] + zl[:-1, 1:, 1:] +
+                  zl[1:, :-1, :-1] + zl[1:, :-1, 1:] + zl[1:, 1:, :-1] + zl[1:, 1:, 1:]).ravel()
+    U = hydrostatic(zc, lz, 998.0) + _rng(5 + seed_offset).normal(0.0, 5e3, nc)
+    info = {"workload": f"spe10_like_hex_{nx}x{ny}x{nz}_jitter{jitter}", "ncells": nc, "seed": MASTER_SEED,
+            "grid": [nx, ny, nz], "extent_m": [lx, ly, lz]}
+    return t, U, info
+
+
+def delaunay_surface(npts, lx, ly, rng):
+    from scipy.spatial import Delaunay
+
+    pts = rng.uniform(0.0, 1.0, (npts, 2)) * [lx, ly]
+    corners = np.array([[0, 0], [lx, 0], [lx, ly], [0, ly]], dtype=float)
+    pts = np.vstack([corners, pts])
+    tri = Delaunay(pts)
+    simp = tri.simplices.astype(np.int32)
+    # counter-clockwise orientation
+    a, b, c = pts[simp[:, 0]], pts[simp[:, 1]], pts[simp[:, 2]]
+    cross = (b[:, 0] - a[:, 0]) * (c[:, 1] - a[:, 1]) - (b[:, 1] - a[:, 1]) * (c[:, 0] - a[:, 0])
+    flip = cross < 0
+    simp[flip] = simp[flip][:, [0, 2, 1]]
+    # drop slivers on the hull (area ~ 0)
+    area = 0.5 * np.abs(cross)
+    keep = area > 1e-9 * lx * ly / max(len(simp), 1)
+    return pts, simp[keep]
+
+
+def random_spd(nc, rng, mean=-12.0, std=1.0):
+    eig = 10.0 ** (mean + std * rng.standard_normal((nc, 3)))
+    q, _ = np.linalg.qr(rng.standard_normal((nc, 3, 3)))
+    K = np.einsum("nij,nj,nkj->nik", q, eig, q)
+    return 0.5 * (K + np.transpose(K, (0, 2, 1)))
+
+
+def wedge_extruded(npts=200, nlayers=4, lx=1000.0, ly=1000.0, seed_offset=0, dz_range=(0.1, 2.0)):
+    """Extruded Delaunay prisms with full-tensor K; returns (tdy, U, info)."""
+    rng = _rng(10 + seed_offset)
+    xy, tris = delaunay_surface(npts, lx, ly, rng)
+    dz = rng.uniform(*dz_range, nlayers)
+    levels = np.concatenate([[0.0], np.cumsum(dz)])
+    z = np.repeat(levels[:, None], xy.shape[0], axis=1)
+    t = create_richards_mpfao()
+    t.set_extruded_mesh(xy, tris, z)
+    t.set_from_options()
+    nc = nlayers * tris.shape[0]
+    t.set_permeability_values(random_spd(nc, _rng(11 + seed_offset)).reshape(nc, 9))
+    r = _rng(12 + seed_offset)
+    t.set_porosity_values(r.uniform(0.05, 0.35, nc))
+    m = r.uniform(0.2, 0.6, nc)
+    t.set_vangenuchten_values(m, 10.0 ** r.uniform(-5.0, -3.0, nc))
+    t.set_mualem_values(m)
+    t.set_water_density_type(WATER_DENSITY_EXPONENTIAL)
+    ztop = levels[-1]
+    t.set_boundary_pressure_type_function(top_dirichlet_types(ztop))
+    t.set_boundary_pressure_function(lambda x, y, zz: PREF - 2e3)
+    layer = np.arange(nc) // tris.shape[0]
+    zc = 0.5 * (levels[layer] + levels[layer + 1])
+    U = hydrostatic(zc, ztop, 998.0) + _rng(13 + seed_offset).normal(0.0, 3e3, nc)
+    return t, U, {"workload": f"wedge_{tris.shape[0]}tri_{nlayers}layers", "ncells": nc}

@@ -1,0 +1,26 @@
+"""Shared test configuration.
+
+Tests marked ``gpu`` need a CUDA device and the built library; everything
+else runs on the CPU.  The oracle (oracle/) is the checker for parity tests.
+"""
+import sys
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA device (GB300) and the built CUDA library")
+
+
+@pytest.fixture(scope="session", autouse=True)
+def _built_libraries():
+    """Build the product library and the oracle once per session (no-op when up to date)."""
+    from tdycore_gb300.build import build_library, build_oracle
+
+    build_library()
+    build_oracle()

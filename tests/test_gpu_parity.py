@@ -1,0 +1,101 @@
+"""GPU residual/Jacobian parity with the oracle (C restatement of the reference).
+
+Tolerances (stated per the spec bar, FP64):
+  residual:  |R_gpu - R_ref| <= 1e-12 * sum_k |terms_k into cell i|  (per cell)
+  Jacobian:  |J_gpu - J_ref| <= 1e-10 * sum_k |contributions_k|      (per entry)
+The right-hand sides are the floating-point error scale of each summed
+quantity (the oracle accumulates the absolute values of every term it adds),
+so cancellation near equilibrium does not make the bar meaningless.  The CSR
+pattern must match the oracle's independently computed pattern bit for bit.
+"""
+import numpy as np
+import pytest
+
+from oracle import Oracle
+from tests.parity_cases import CASES
+
+pytestmark = pytest.mark.gpu
+
+R_TOL = 1e-12
+J_TOL = 1e-10
+DT = 1800.0
+
+
+def _setup(name):
+    t, U, Uprev, Ut = CASES[name]()
+    t.setup()
+    o = Oracle(t.setup_view())
+    return t, o, U, Uprev, Ut
+
+
+def assert_close(got, ref, mag, tol, what):
+    err = np.abs(got - ref)
+    bound = tol * np.maximum(mag, np.finfo(float).tiny)
+    bad = np.nonzero(err > bound)[0]
+    assert bad.size == 0, (f"{what}: {bad.size} entries out of tolerance; worst index {bad[np.argmax(err[bad] / bound[bad])]}"
+                           f" err {err[bad].max():.3e} mag {mag[bad].max():.3e}")
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_snes_parity(name):
+    t, o, U, Uprev, _ = _setup(name)
+    rp, ci = o.pattern()
+    assert np.array_equal(rp, t.rowptr) and np.array_equal(ci, t.colidx), "CSR pattern differs"
+    t.set_dtime(DT)
+    t.presolve(Uprev)
+    o.snes_presolve(Uprev, DT)
+    R, J = t.snes_function_jacobian(U)
+    Rr, Rm = o.snes_function(U, with_mag=True)
+    Jr, Jm = o.snes_jacobian(U, with_mag=True)
+    assert_close(R, Rr, Rm, R_TOL, f"{name} SNES residual")
+    assert_close(J, Jr, Jm, J_TOL, f"{name} SNES Jacobian")
+    # separate entry points agree with the fused one bit for bit
+    assert np.array_equal(t.snes_function(U), R)
+    assert np.array_equal(t.snes_jacobian(U), J)
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_ts_parity(name):
+    t, o, U, _, Ut = _setup(name)
+    shift = 1.0 / 100.0
+    R, J = t.ifunction_ijacobian(0.0, U, Ut, shift)
+    Rr, Rm = o.ts_ifunction(U, Ut, with_mag=True)
+    Jr, Jm = o.ts_ijacobian(U, Ut, shift, with_mag=True)
+    assert_close(R, Rr, Rm, R_TOL, f"{name} TS residual")
+    assert_close(J, Jr, Jm, J_TOL, f"{name} TS Jacobian")
+
+
+def test_deterministic_and_device_entry_point():
+    import torch
+
+    t, o, U, Uprev, _ = _setup("spe10_small")
+    t.set_dtime(DT)
+    t.presolve(Uprev)
+    R1, J1 = t.snes_function_jacobian(U)
+    R2, J2 = t.snes_function_jacobian(U)
+    assert np.array_equal(R1, R2) and np.array_equal(J1, J2)
+    dU = torch.tensor(U, dtype=torch.float64, device="cuda")
+    dR = torch.empty(t.ncells, dtype=torch.float64, device="cuda")
+    dJ = torch.empty(t.nnz, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream()
+    t.snes_function_jacobian_device(dU, dR, dJ, stream=stream.cuda_stream)
+    torch.cuda.synchronize()
+    assert np.array_equal(dR.cpu().numpy(), R1)
+    assert np.array_equal(dJ.cpu().numpy(), J1)
+
+
+def test_jacobian_is_derivative_of_residual():
+    """Central differences of the GPU residual against the GPU Jacobian."""
+    t, o, U, Uprev, _ = _setup("spe10_small")
+    t.set_dtime(DT)
+    t.presolve(Uprev)
+    R, J = t.snes_function_jacobian(U)
+    n = t.ncells
+    rng = np.random.default_rng(11)
+    d = rng.standard_normal(n)
+    eps = 1e-3
+    fd = (t.snes_function(U + eps * d) - t.snes_function(U - eps * d)) / (2 * eps)
+    rows = np.repeat(np.arange(n), np.diff(t.rowptr))
+    Jd = np.bincount(rows, weights=J * d[t.colidx], minlength=n)
+    scale = np.abs(Jd).max()
+    assert np.abs(fd - Jd).max() <= 1e-5 * scale
