@@ -38,9 +38,13 @@ class OracleInput(ctypes.Structure):
 
 def _load():
     if not _LIB.exists():
-        from tdycore_gb300.build import build_oracle  # build recipe only; no evaluation code
+        import importlib.util
 
-        build_oracle()
+        spec = importlib.util.spec_from_file_location("tdycore_gb300_build",
+                                                      _HERE.parent / "tdycore_gb300" / "build.py")
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        mod.build_oracle()
     lib = ctypes.CDLL(str(_LIB))
     lib.oracle_create.restype = c_void_p
     lib.oracle_create.argtypes = [POINTER(OracleInput)]

@@ -20,7 +20,6 @@ def pytest_configure(config):
 @pytest.fixture(scope="session", autouse=True)
 def _built_libraries():
     """Build the product library and the oracle once per session (no-op when up to date)."""
-    from tdycore_gb300.build import build_library, build_oracle
+    import __graft_entry__
 
-    build_library()
-    build_oracle()
+    __graft_entry__.build()
