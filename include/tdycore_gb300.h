@@ -185,6 +185,23 @@ TDyErrorCode TDyMPFAOSNESFunctionJacobianDevice(TDy tdy, const double *dU, doubl
 TDyErrorCode TDyMPFAOIFunctionIJacobianDevice(TDy tdy, double t, const double *dU, const double *dU_t, double shift,
                                               double *dR, double *dJ, void *stream);
 TDyErrorCode TDyPreSolveSNESSolverDevice(TDy tdy, const double *dU_prev, void *stream);
+/* Same result as TDyMPFAOSNESFunctionJacobianDevice, but the call allocates
+ * no device memory at all: its partial-sum scratch is a fixed 64 MiB array
+ * built into the library (8,388,608 doubles; every GPU that loads the library
+ * keeps it until the process exits) rather than memory belonging to the
+ * handle.  Meant for callers that are not allowed to allocate on the device
+ * while they run, such as a host application whose device memory is handed
+ * out by its own pool and must not change behind its back, or a time-critical
+ * loop that cannot afford the device-wide synchronisation cudaMalloc and
+ * cudaFree may cause.  The caller passes inputs and outputs as device
+ * pointers.  Meshes whose scratch would exceed the array (about 110,000
+ * interior hexahedral vertices) are rejected with TDY_ERR_ARG_OUTOFRANGE.
+ * The first call on a device looks up the array's device address, so make
+ * that first call before capturing any stream.  All calls share the array:
+ * calls that overlap on the GPU race and must be serialised by the caller.
+ * This entry point has no counterpart in the reference. */
+TDyErrorCode TDyMPFAOSNESFunctionJacobianDeviceNoAlloc(TDy tdy, const double *dU, double *dR, double *dJ,
+                                                       void *stream);
 /* Number of hot-path kernel launches one ...Device call enqueues. */
 TDyErrorCode TDyGetLaunchesPerEvaluation(TDy tdy, int *nlaunch);
 TDyErrorCode TDySynchronize(TDy tdy);

@@ -128,6 +128,7 @@ _sig("TDyMPFAOSNESFunctionJacobianDevice", c_void_p, c_void_p, c_void_p, c_void_
 _sig("TDyMPFAOIFunctionIJacobianDevice", c_void_p, c_double, c_void_p, c_void_p, c_double, c_void_p, c_void_p,
      c_void_p)
 _sig("TDyPreSolveSNESSolverDevice", c_void_p, c_void_p, c_void_p)
+_sig("TDyMPFAOSNESFunctionJacobianDeviceNoAlloc", c_void_p, c_void_p, c_void_p, c_void_p, c_void_p)
 _sig("TDyGetLaunchesPerEvaluation", c_void_p, _ip)
 _sig("TDySynchronize", c_void_p)
 _sig("TDyUpdateState", c_void_p, _dp, c_int)

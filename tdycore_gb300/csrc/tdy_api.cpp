@@ -880,6 +880,13 @@ TDyErrorCode TDyMPFAOIFunctionIJacobianDevice(TDy tdy, double t, const double *d
   if (!dU || !dU_t || (!dR && !dJ)) return set_error(TDY_ERR_ARG_NULL, "null array");
   return device_eval(tdy, FORM_TS, t, dU, dU_t, shift, dR, dJ, stream);
 }
+TDyErrorCode TDyMPFAOSNESFunctionJacobianDeviceNoAlloc(TDy tdy, const double *dU, double *dR, double *dJ,
+                                                       void *stream) {
+  TDY_CHECK_HANDLE(tdy);
+  TDY_CHECK_DEVICE(tdy);
+  if (!dU || (!dR && !dJ)) return set_error(TDY_ERR_ARG_NULL, "null array");
+  return device_eval_noalloc(tdy, dU, dR, dJ, stream);
+}
 TDyErrorCode TDyPreSolveSNESSolverDevice(TDy tdy, const double *dU_prev, void *stream) {
   TDY_CHECK_HANDLE(tdy);
   TDY_CHECK_DEVICE(tdy);

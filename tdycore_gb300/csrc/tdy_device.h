@@ -23,5 +23,6 @@ int device_get_diagnostic(_p_TDy *t, int which, double *out);
 int device_set_timers(_p_TDy *t, int on);
 int device_get_timers(_p_TDy *t, int *n, const char **names, double *ms, long long *calls);
 int device_fp64_probe(double *tflops);
+int device_eval_noalloc(_p_TDy *t, const double *dU, double *dR, double *dJ, void *stream);
 
 }  // namespace tdy

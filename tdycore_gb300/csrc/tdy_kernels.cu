@@ -26,6 +26,7 @@
 
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <type_traits>
 #include <vector>
 
@@ -81,6 +82,7 @@ struct DeviceState {
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   double t_ms[3] = {0, 0, 0};
   long long t_calls[3] = {0, 0, 0};
+  int device = 0;  // CUDA device current at TDySetup
   // owned allocations
   std::vector<void *> allocs;
   double *dU = nullptr, *dUt = nullptr, *dR = nullptr, *dJ = nullptr;
@@ -449,6 +451,7 @@ int device_setup(_p_TDy *t) {
     return set_error(TDY_ERR_GPU, "no CUDA device available: %s", e != cudaSuccess ? cudaGetErrorString(e) : "0 devices");
   DeviceState *d = new DeviceState();
   t->dev = d;
+  CUDA_TRY(cudaGetDevice(&d->device));
   CUDA_TRY(cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking));
   DevArgs &a = d->a;
   memset(&a, 0, sizeof(a));
@@ -693,6 +696,72 @@ int device_eval_host(_p_TDy *t, int form, double time, const double *U, const do
   if (R) CUDA_TRY(cudaMemcpyAsync(R, d->dR, sizeof(double) * n, cudaMemcpyDeviceToHost, d->stream));
   if (J) CUDA_TRY(cudaMemcpyAsync(J, d->dJ, sizeof(double) * d->nnz, cudaMemcpyDeviceToHost, d->stream));
   CUDA_TRY(cudaStreamSynchronize(d->stream));
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Evaluation without any device allocation of its own.
+//
+// The per-vertex partial sums (J_v, R_v) normally live in scratch that
+// TDySetup allocates for the handle.  This variant takes them from a fixed
+// array compiled into the library instead, so nothing in it allocates device
+// memory.  The array is 64 MiB of doubles; every GPU that loads the library
+// holds it until the process exits.  Host code never uses the array's name as
+// an address (on the host it is only a stand-in for the symbol): the device
+// address is looked up once per device with cudaGetSymbolAddress while that
+// device is current, on the first call made on it.
+//
+// All calls share the array and it keeps the last call's contents.  Nothing
+// has to start at zero: vertex_kernel writes every partial that cell_kernel
+// then reads in the same call.  Calls that overlap on the GPU (two streams, or
+// two handles at once) race on the array and must be serialised by the caller.
+#define TDY_NOALLOC_SCRATCH_DOUBLES (8ull << 20)
+#define TDY_NOALLOC_MAX_DEVICES 64
+static __device__ __align__(256) double g_noalloc_scratch[TDY_NOALLOC_SCRATCH_DOUBLES];
+static double *g_noalloc_ptr[TDY_NOALLOC_MAX_DEVICES] = {};
+static std::mutex g_noalloc_mutex;
+
+int device_eval_noalloc(_p_TDy *t, const double *dU, double *dR, double *dJ, void *stream) {
+  DeviceState *d = t->dev;
+  const long long need = t->setup.v_jv_off[t->mesh.nv];
+  if (need > (long long)TDY_NOALLOC_SCRATCH_DOUBLES)
+    return set_error(TDY_ERR_ARG_OUTOFRANGE,
+                     "mesh needs %lld doubles of partial-sum scratch; the static scratch holds %llu (64 MiB). "
+                     "Use TDyMPFAOSNESFunctionJacobianDevice for meshes this large",
+                     need, (unsigned long long)TDY_NOALLOC_SCRATCH_DOUBLES);
+  if (!(t->dtime > 0.0)) return set_error(TDY_ERR_USER, "SNES form needs TDySetDtimeForSNESSolver before evaluation");
+  int dev = -1;
+  CUDA_TRY(cudaGetDevice(&dev));
+  if (dev != d->device)
+    return set_error(TDY_ERR_USER, "current CUDA device %d is not the device %d this handle was set up on", dev,
+                     d->device);
+  if (dev < 0 || dev >= TDY_NOALLOC_MAX_DEVICES) return set_error(TDY_ERR_SUP, "device ordinal %d not supported", dev);
+  double *scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+      void *p = nullptr;
+      CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+      g_noalloc_ptr[dev] = (double *)p;
+    }
+    scratch = g_noalloc_ptr[dev];
+  }
+  cudaStream_t st = stream ? (cudaStream_t)stream : d->stream;
+  DevArgs a = d->a;
+  a.form = FORM_SNES;
+  a.U = dU;
+  a.Ut = nullptr;
+  a.dt = t->dtime;
+  a.shift = 0.0;
+  a.needR = dR != nullptr;
+  a.needJ = dJ != nullptr;
+  a.R = dR;
+  a.J = dJ;
+  a.scratch = scratch;
+  state_kernel<<<nblocks(a.nc + a.nb, 256), 256, 0, st>>>(a);
+  vertex_kernel<<<nblocks(a.nv, 128), 128, 0, st>>>(a);
+  cell_kernel<<<nblocks(a.nc, 128), 128, 0, st>>>(a);
+  CUDA_TRY(cudaGetLastError());
   return 0;
 }
 
