@@ -109,13 +109,17 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def build_workload(host_only=False):
+def build_workload(host_only=False, grid=None):
     import tdycore_gb300 as T
     from tdycore_gb300.workloads import spe10_like
 
     T.options_clear()
     t0 = time.perf_counter()
-    t, U, info = spe10_like()
+    if grid:
+        nx, ny, nz = grid
+        t, U, info = spe10_like(nx, ny, nz, lx=365.76 * nx / 60, ly=670.56 * ny / 220, lz=51.816 * nz / 85)
+    else:
+        t, U, info = spe10_like()
     t.setup(host_only=host_only)
     log(f"setup: {info['workload']} {t.ncells} cells, nnz {t.nnz}, {time.perf_counter() - t0:.1f} s")
     rng = np.random.default_rng(20261203)
@@ -180,7 +184,7 @@ def cpu_baseline(view, U, Uprev, budget_s=12.0, threads=None):
 def run_reference(args, rank):
     if rank != 0:
         return
-    t, U, Uprev, info = build_workload(host_only=True)
+    t, U, Uprev, info = build_workload(host_only=True, grid=args.grid)
     view = t.setup_view()
     from oracle import Oracle
 
@@ -220,7 +224,7 @@ def run_gpu(args, rank, world, local_rank):
         import torch.distributed as dist
 
         dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
-    t, U, Uprev, info = build_workload()
+    t, U, Uprev, info = build_workload(grid=args.grid)
     view = t.setup_view()
     nc, nnz = t.ncells, t.nnz
     t.set_dtime(DT)
@@ -247,7 +251,7 @@ def run_gpu(args, rank, world, local_rank):
             t.snes_function_jacobian_device(dU, dR, dJ, stream=sp)
         e1.record(stream)
         torch.cuda.synchronize(dev)
-        if args.steps * 0.001 < 1.0:  # keep sampling ~1 s of load for the clock record
+        if not args.profile and args.steps * 0.001 < 1.0:  # keep ~1 s of load for the clock record
             tt = time.perf_counter()
             while time.perf_counter() - tt < 1.0:
                 t.snes_function_jacobian_device(dU, dR, dJ, stream=sp)
@@ -260,6 +264,10 @@ def run_gpu(args, rank, world, local_rank):
     ms_per_step = ms / args.steps
     value = world * nc * args.steps / (ms * 1e-3)
 
+    if args.profile:
+        if rank == 0:
+            print(json.dumps({"profile_run": info["workload"], "ncells": nc, "ms_per_step": ms / args.steps}))
+        return
     # per-kernel durations (events between launches)
     t.set_timers(True)
     kt_steps = min(args.steps, 50)
@@ -348,6 +356,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=12.0)
+    ap.add_argument("--grid", type=int, nargs=3, default=None, metavar=("NX", "NY", "NZ"),
+                    help="smaller grid with the same extents per cell (profiling captures)")
+    ap.add_argument("--profile", action="store_true",
+                    help="time the device loop only (no timers, e2e, CPU or clock-fill loops), for ncu")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
