@@ -122,17 +122,39 @@ struct MPFAOSetup {
   std::vector<double> gravdis;                    // nf
   // Jacobian pattern
   std::vector<int> rowptr, colidx;
-  // cell -> (vertex, local index, slot map) gather program
+  // Canonical interior hexahedral vertices: 8 cells, 12 internal faces, no
+  // boundary column, cells indexed by octant (bit0 x, bit1 y, bit2 z relative
+  // to the vertex) and rows in the fixed order of kCanonUp/kCanonDn, with the
+  // face's first cell on the lower side.  Stored structure-of-arrays with
+  // stride nCpad so consecutive threads read consecutive vertices.
+  int nC = 0, nCpad = 0;
+  std::vector<int> canon_vertex;   // nC
+  std::vector<double> Tc;          // 96 * nCpad, entry (row*8 + col)
+  std::vector<int> cellc;          // 8 * nCpad
+  std::vector<int> facec;          // 12 * nCpad
+  std::vector<int> gen_vertex;     // other vertices with cells (generic path)
+  // Scratch: canonical partials SoA [72][nCpad] (J_v row-major then R_v),
+  // then generic per-vertex blocks J_v[nint][nint], R_v[nint].
+  std::vector<long long> v_jv_off; // nv: generic block offset, or canonical column index
+  long long scratch_size = 0;
+  // cell -> (vertex) gather program
   std::vector<int> cv_off;         // nc+1
-  std::vector<int> cv_vertex;      // per (cell, vertex)
-  std::vector<int> cv_local;       // local internal-cell index of the cell at that vertex
+  std::vector<long long> cv_jbase; // offset of J_v[a][0] in scratch
+  std::vector<long long> cv_rbase; // offset of R_v[a]
+  std::vector<int> cv_stride;      // distance between J_v[a][b] and J_v[a][b+1]
+  std::vector<int> cv_nint;        // columns of the vertex
+  std::vector<int> cv_local;       // a: local index of the cell at the vertex
   std::vector<int> cv_slot_off;    // offset into cv_slots for this (cell, vertex)
-  std::vector<uint8_t> cv_slots;   // CSR slot (within the row) of each internal column
-  std::vector<long long> v_jv_off; // nv+1: scratch offsets (nint*nint + nint doubles)
+  std::vector<uint8_t> cv_slots;   // CSR slot (within the row) of each vertex column
   int max_nint = 0, max_nrow = 0, max_ncol = 0, max_row_nnz = 0;
 };
 
 int mpfao_setup(const Options &opt, const Mesh &m, const Materials &mat, const Boundary &bnd, MPFAOSetup &s);
+
+// Canonical interior-hex row order: row r joins octants kCanonUp[r] (lower
+// side, the face's first cell) and kCanonDn[r] = kCanonUp[r] | (1 << (r / 4)).
+constexpr int kCanonUp[12] = {0, 2, 4, 6, 0, 1, 4, 5, 0, 1, 2, 3};
+constexpr int kCanonDn[12] = {1, 3, 5, 7, 2, 3, 6, 7, 4, 5, 6, 7};
 
 // EOS at one pressure (src/materials/tdyeos.c:5-136).
 void eos_density(int type, double p, double *rho, double *drho, double *d2rho);

@@ -1,7 +1,7 @@
 // tdy_kernels.cu -- sm_103a kernels of the MPFA-O Richards residual and
 // Jacobian, and their host-side launch code.
 //
-// One evaluation is three launches on one stream:
+// One evaluation is four launches on one stream:
 //   1. state_kernel   (cells, then boundary faces)
 //        TDyUpdateState_Richards_MPFAO (src/fv/mpfao/tdympfao.c:2527-2594),
 //        TDyMPFAO_SetBoundaryPressure + TDyMPFAOUpdateBoundaryState
@@ -9,19 +9,29 @@
 //        terms of TDyMPFAOSNESFunction/Jacobian (tdympfao_snes.c:19-30,
 //        112-123, 166-179) or TDyMPFAOIFunction/IJacobian_Accumulation
 //        (tdympfao_ts.c:191-212, 459-517).
-//   2. vertex_kernel  (one thread per vertex)
+//   2. canon_vertex_kernel  (one thread per interior hexahedral vertex)
+//   3. vertex_kernel        (one thread per other vertex)
 //        MatMult(Trans_mat, P_vec) (tdympfao_ts.c:184) restricted to the
 //        vertex's rows, the upwinded flux of TDyMPFAOIFunction_Vertices
 //        (tdympfao_ts.c:12-150) and the Jacobian entries of
 //        TDyMPFAOIJacobian_Vertices (tdympfao_ts.c:235-456).  Each vertex
 //        writes its partial residual R_v[nint] and partial Jacobian block
 //        J_v[nint][nint] (rows and columns: the vertex's internal cells) to a
-//        scratch area it alone owns.
-//   3. cell_kernel    (one thread per cell)
+//        scratch area it alone owns.  Interior hexahedral vertices use a fixed
+//        octant layout (rows and columns known at compile time, structure-of-
+//        arrays storage read with coalesced loads); the rest use per-vertex
+//        blocks.
+//   4. cell_kernel    (one thread per cell)
 //        sums, in a fixed order, the partials of the cell's vertices into
 //        R[cell] and into the cell's row of the fixed CSR pattern, then adds
 //        the accumulation terms.  No atomics: results are bitwise
 //        reproducible run to run.
+//
+// Per row the flux is evaluated as -w*(T.P + rho_avg*G) with w = rho_avg*kr/mu
+// and the Jacobian entry as -(w*T + E) with E the derivative terms of the
+// up/down cell, the same quantities as the reference's
+// rho*kr/mu*(-T.P) - rho^2*kr/mu*G and its five-term derivative
+// (tdympfao_ts.c:116-118, 404-417) regrouped to need fewer FP64 operations.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -52,36 +62,45 @@ struct DevArgs {
   // boundary faces
   const int *bnd_cell, *bnd_type, *bnd_has;
   const double *bnd_val, *bnd_rho, *bnd_vis;
-  // extended state (cells then boundary faces)
-  double *P, *rho, *drho, *lam, *dlam;
+  // extended state (cells then boundary faces): P, rho/2, (drho/dP)/2, kr/mu,
+  // d(kr/mu)/dP, seepage flag
+  double *P, *hr, *hdr, *lam, *dlam;
   unsigned char *seep;
   double *acc_a, *acc_b, *jdiag;
   // faces
   const int *f_up, *f_dn;
   const double *G;
-  // vertices
+  // canonical interior-hex vertices (SoA, stride nCpad)
+  int nC, nCpad;
+  const double *Tc;
+  const int *cellc, *facec;
+  // generic vertices
+  int ngen;
+  const int *gen_vertex;
   const int *v_row_off, *v_col_off, *v_nint;
   const long long *v_trans_off, *v_jv_off;
   const int *row_face, *row_lup, *row_ldn, *col_ext;
   const double *trans;
   double *scratch;
   // cell gather
-  const int *rowptr, *cv_off, *cv_vertex, *cv_local, *cv_slot_off;
+  const int *rowptr, *cv_off, *cv_stride, *cv_nint, *cv_local, *cv_slot_off;
+  const long long *cv_jbase, *cv_rbase;
   const unsigned char *cv_slots;
+  int max_row_nnz;
   // outputs
   double *R, *J;
 };
 
-static const char *const kKernelNames[3] = {"state_kernel", "vertex_kernel", "cell_kernel"};
+static const char *const kKernelNames[4] = {"state_kernel", "canon_vertex_kernel", "vertex_kernel", "cell_kernel"};
 
 struct DeviceState {
   cudaStream_t stream = nullptr;
   DevArgs a;
   // per-kernel timers (TDY_START_FUNCTION_TIMER analogue, include/tdytimers.h)
   bool timers = false;
-  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
-  double t_ms[3] = {0, 0, 0};
-  long long t_calls[3] = {0, 0, 0};
+  cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  double t_ms[4] = {0, 0, 0, 0};
+  long long t_calls[4] = {0, 0, 0, 0};
   int device = 0;  // CUDA device current at TDySetup
   // owned allocations
   std::vector<void *> allocs;
@@ -230,8 +249,8 @@ __global__ void __launch_bounds__(256) state_kernel(DevArgs a) {
     density(a.rho_type, P, &rho, &drho, &d2rho);
     viscosity(a.mu_type, &vis, &dvis);
     a.P[i] = P;
-    a.rho[i] = rho;
-    a.drho[i] = drho;
+    a.hr[i] = 0.5 * rho;
+    a.hdr[i] = 0.5 * drho;
     a.lam[i] = Kr / vis;
     a.dlam[i] = dKr_dS * dS / vis - Kr / (vis * vis) * dvis;
     a.seep[i] = 0;
@@ -263,8 +282,8 @@ __global__ void __launch_bounds__(256) state_kernel(DevArgs a) {
     double Kr, dKr;
     relperm(a.rp_type[c], a.rp_param + 9 * (size_t)c, Se, &Kr, &dKr);
     a.P[i] = p;
-    a.rho[i] = a.bnd_rho[b];
-    a.drho[i] = 0.0;
+    a.hr[i] = 0.5 * a.bnd_rho[b];
+    a.hdr[i] = 0.0;
     a.lam[i] = Kr / a.bnd_vis[b];
     a.dlam[i] = 0.0;
     a.seep[i] = (a.bnd_type[b] == SEEPAGE_BC && p <= a.Pref) ? 1 : 0;
@@ -301,12 +320,119 @@ __global__ void __launch_bounds__(256) diag_kernel(DevArgs a, double *Sout, doub
 }
 
 // ---------------------------------------------------------------------------
-// 2. per-vertex flux and Jacobian partials
+// 2. interior hexahedral vertices, octant layout
+
+// Octants joined by canonical row r (kCanonUp/kCanonDn in tdy_internal.h).
+__host__ __device__ constexpr int canon_up(int r) {
+  return r < 4 ? 2 * r : r < 8 ? (((r - 4) & 1) | (((r - 4) >> 1) << 2)) : r - 8;
+}
+__host__ __device__ constexpr int canon_dn(int r) { return canon_up(r) | (1 << (r / 4)); }
+static_assert(canon_up(5) == kCanonUp[5] && canon_dn(5) == kCanonDn[5] && canon_up(10) == kCanonUp[10] &&
+                  canon_dn(10) == kCanonDn[10] && canon_up(2) == kCanonUp[2] && canon_dn(7) == kCanonDn[7],
+              "canonical row tables disagree");
+
+// Row of the canonical layout that joins octant c with its neighbour across
+// axis k, and whether c is that row's first ("up") cell.
+__host__ __device__ constexpr int canon_row(int c, int k) {
+  return k == 0 ? ((c & ~1) >> 1) : k == 1 ? 4 + (((c & ~2) & 1) | (((c & ~2) >> 2) << 1)) : 8 + (c & ~4);
+}
+__host__ __device__ constexpr bool canon_is_up(int c, int k) { return ((c >> k) & 1) == 0; }
+
+template <bool CONST_RHO>
+__global__ void __launch_bounds__(128) canon_vertex_kernel(DevArgs a) {
+  extern __shared__ double sh[];  // [36][blockDim]: w, E_up, E_dn per row
+  const int tid = threadIdx.x, bs = blockDim.x;
+  const int vc = blockIdx.x * bs + tid;
+  if (vc >= a.nC) return;
+  const long long P = a.nCpad;
+  double p[8], hr[8], lam[8], dlam[8], hdr[8];
+#pragma unroll
+  for (int o = 0; o < 8; o++) {
+    const int cell = a.cellc[o * P + vc];
+    p[o] = a.P[cell];
+    hr[o] = a.hr[cell];
+    lam[o] = a.lam[cell];
+    dlam[o] = a.dlam[cell];
+    hdr[o] = CONST_RHO ? 0.0 : a.hdr[cell];
+  }
+  double Rv[8];
+#pragma unroll
+  for (int o = 0; o < 8; o++) Rv[o] = 0.0;
+#pragma unroll
+  for (int r = 0; r < 12; r++) {
+    const int u = canon_up(r), d = canon_dn(r);
+    const double *T = a.Tc + (long long)(r * 8) * P + vc;
+    double TP = 0.0;
+#pragma unroll
+    for (int c = 0; c < 8; c++) TP += T[c * P] * p[c];
+    const double G = a.G[a.facec[r * P + vc]];
+    const double den = hr[u] + hr[d];
+    const double q = TP + den * G;
+    const bool fdn = q < 0.0;
+    const double lm = fdn ? lam[u] : lam[d];
+    const double w = den * lm;
+    const double flux = -(w * q);
+    Rv[u] += flux;
+    Rv[d] -= flux;
+    if (a.needJ) {
+      const double dlu = fdn ? dlam[u] : 0.0, dld = fdn ? 0.0 : dlam[d];
+      double eu, ed;
+      if (CONST_RHO) {
+        eu = den * dlu * q;
+        ed = den * dld * q;
+      } else {
+        const double g2 = q + den * G;
+        eu = hdr[u] * lm * g2 + den * dlu * q;
+        ed = hdr[d] * lm * g2 + den * dld * q;
+      }
+      sh[r * bs + tid] = w;
+      sh[(12 + r) * bs + tid] = eu;
+      sh[(24 + r) * bs + tid] = ed;
+    }
+  }
+  double *S = a.scratch;
+  if (a.needR) {
+#pragma unroll
+    for (int c = 0; c < 8; c++) S[(64 + c) * P + vc] = Rv[c];
+  }
+  if (a.needJ) {
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+      double acc[8];
+#pragma unroll
+      for (int b = 0; b < 8; b++) acc[b] = 0.0;
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        const int r = canon_row(c, k);
+        const bool up = canon_is_up(c, k);
+        const double wr = sh[r * bs + tid];
+        const double sw = up ? -wr : wr;
+        const double *T = a.Tc + (long long)(r * 8) * P + vc;
+#pragma unroll
+        for (int b = 0; b < 8; b++) acc[b] = fma(sw, T[b * P], acc[b]);
+        const double eu = sh[(12 + r) * bs + tid], ed = sh[(24 + r) * bs + tid];
+        const int u = canon_up(r), d = canon_dn(r);
+        if (up) {
+          acc[u] -= eu;
+          acc[d] -= ed;
+        } else {
+          acc[u] += eu;
+          acc[d] += ed;
+        }
+      }
+#pragma unroll
+      for (int b = 0; b < 8; b++) S[(c * 8 + b) * P + vc] = acc[b];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// 3. other vertices: per-vertex blocks
 __global__ void __launch_bounds__(128) vertex_kernel(DevArgs a) {
-  const int v = blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= a.nv) return;
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= a.ngen) return;
+  const int v = a.gen_vertex[g];
   const int nint = a.v_nint[v];
-  if (nint == 0) return;
   const int r0 = a.v_row_off[v], nrow = a.v_row_off[v + 1] - r0;
   const int c0 = a.v_col_off[v], ncol = a.v_col_off[v + 1] - c0;
   const double *T = a.trans + a.v_trans_off[v];
@@ -321,29 +447,24 @@ __global__ void __launch_bounds__(128) vertex_kernel(DevArgs a) {
     const int f = a.row_face[r0 + r];
     const int up = a.f_up[f], dn = a.f_dn[f];
     const double G = a.G[f];
-    const double den = (a.rho[up] + a.rho[dn]) * 0.5;
-    const bool flowdn = (TP + den * G < 0.0);
+    const double den = a.hr[up] + a.hr[dn];
+    const double q = TP + den * G;
+    const bool flowdn = q < 0.0;
     const int u = flowdn ? up : dn;
-    const double ukvr = a.lam[u];
+    const double lm = a.lam[u];
     const bool zero = a.seep[u] != 0;
-    double fluxm = 0.0;
-    if (!zero) {
-      fluxm = den * ukvr * (-TP);
-      fluxm += -(den * den) * ukvr * G;
-    }
-    fl[r] = fluxm;
+    const double wr = zero ? 0.0 : den * lm;
+    fl[r] = -(wr * q);
     if (a.needJ) {
+      w[r] = wr;
       if (zero) {
-        w[r] = 0.0;
         Eu[r] = 0.0;
         Ed[r] = 0.0;
       } else {
-        const double dden_up = 0.5 * a.drho[up], dden_dn = 0.5 * a.drho[dn];
-        const double dukvr_up = flowdn ? a.dlam[up] : 0.0;
-        const double dukvr_dn = flowdn ? 0.0 : a.dlam[dn];
-        w[r] = den * ukvr;
-        Eu[r] = dden_up * ukvr * TP + den * dukvr_up * TP + (2 * den * dden_up * ukvr * G + (den * den) * dukvr_up * G);
-        Ed[r] = dden_dn * ukvr * TP + den * dukvr_dn * TP + (2 * den * dden_dn * ukvr * G + (den * den) * dukvr_dn * G);
+        const double dlu = flowdn ? a.dlam[up] : 0.0, dld = flowdn ? 0.0 : a.dlam[dn];
+        const double g2 = q + den * G;
+        Eu[r] = a.hdr[up] * lm * g2 + den * dlu * q;
+        Ed[r] = a.hdr[dn] * lm * g2 + den * dld * q;
       }
     }
   }
@@ -358,64 +479,64 @@ __global__ void __launch_bounds__(128) vertex_kernel(DevArgs a) {
     }
   }
   if (a.needJ) {
-    int lst[TDY_MAX_ROWS];
     for (int c = 0; c < nint; c++) {
-      int nl = 0;
+      for (int b = 0; b < nint; b++) Jv[c * nint + b] = 0.0;
       for (int r = 0; r < nrow; r++) {
-        if (a.row_lup[r0 + r] == c) lst[nl++] = r;
-        if (a.row_ldn[r0 + r] == c) lst[nl++] = -(r + 1);
-      }
-      for (int b = 0; b < nint; b++) {
-        double acc = 0.0;
-        for (int k = 0; k < nl; k++) {
-          const bool is_up = lst[k] >= 0;
-          const int r = is_up ? lst[k] : -lst[k] - 1;
-          double jac = w[r] * T[(size_t)r * ncol + b];
-          if (a.row_lup[r0 + r] == b) jac += Eu[r];
-          if (a.row_ldn[r0 + r] == b) jac += Ed[r];
-          jac = -jac;
-          acc += is_up ? jac : -jac;
-        }
-        Jv[c * nint + b] = acc;
+        const int lu = a.row_lup[r0 + r], ld = a.row_ldn[r0 + r];
+        if (lu != c && ld != c) continue;
+        const double sw = (lu == c) ? -w[r] : w[r];
+        const double *Tr = T + (size_t)r * ncol;
+        for (int b = 0; b < nint; b++) Jv[c * nint + b] = fma(sw, Tr[b], Jv[c * nint + b]);
+        const double s = (lu == c) ? -1.0 : 1.0;
+        if (lu >= 0) Jv[c * nint + lu] += s * Eu[r];
+        if (ld >= 0) Jv[c * nint + ld] += s * Ed[r];
       }
     }
   }
 }
 
 // ---------------------------------------------------------------------------
-// 3. per-cell deterministic gather into R and the CSR row
-__global__ void __launch_bounds__(128) cell_kernel(DevArgs a) {
+// 4. per-cell deterministic gather into R and the CSR row.  Each warp stages
+// its 32 consecutive rows (contiguous in the CSR value array) in shared memory
+// and writes them out with coalesced stores.
+__global__ void __launch_bounds__(64) cell_kernel(DevArgs a) {
+  extern __shared__ double rowbuf[];  // [warps][32 * max_row_nnz]
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.nc) return;
-  const int k0 = a.cv_off[i], k1 = a.cv_off[i + 1];
-  if (a.needR) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int i0 = i - lane;
+  if (i0 >= a.nc) return;  // whole warp out of range
+  const bool active = i < a.nc;
+  if (a.needR && active) {
+    const int k0 = a.cv_off[i], k1 = a.cv_off[i + 1];
     double s = 0.0;
-    for (int k = k0; k < k1; k++) {
-      const int v = a.cv_vertex[k];
-      const int nint = a.v_nint[v];
-      s += a.scratch[a.v_jv_off[v] + (long long)nint * nint + a.cv_local[k]];
-    }
+    for (int k = k0; k < k1; k++) s += a.scratch[a.cv_rbase[k]];
     s += a.acc_a[i];
     s -= a.acc_b[i];
     a.R[i] = s;
   }
-  if (a.needJ) {
+  if (!a.needJ) return;
+  const int iend = min(i0 + 32, a.nc);
+  const int base = a.rowptr[i0];
+  double *buf = rowbuf + (size_t)warp * 32 * a.max_row_nnz;
+  if (active) {
     const int p0 = a.rowptr[i], rn = a.rowptr[i + 1] - p0;
-    double row[TDY_MAX_ROW_NNZ];
+    double *row = buf + (p0 - base);
     for (int j = 0; j < rn; j++) row[j] = 0.0;
+    const int k0 = a.cv_off[i], k1 = a.cv_off[i + 1];
     int diag = -1;
     for (int k = k0; k < k1; k++) {
-      const int v = a.cv_vertex[k];
-      const int nint = a.v_nint[v];
-      const double *blk = a.scratch + a.v_jv_off[v] + (long long)a.cv_local[k] * nint;
+      const int nint = a.cv_nint[k], stride = a.cv_stride[k];
+      const double *blk = a.scratch + a.cv_jbase[k];
       const unsigned char *sl = a.cv_slots + a.cv_slot_off[k];
-      for (int b = 0; b < nint; b++) row[sl[b]] += blk[b];
+      for (int b = 0; b < nint; b++) row[sl[b]] += blk[(long long)b * stride];
       diag = sl[a.cv_local[k]];
     }
     if (diag >= 0) row[diag] += a.jdiag[i];
-    double *out = a.J + p0;
-    for (int j = 0; j < rn; j++) out[j] = row[j];
   }
+  __syncwarp();
+  const int total = a.rowptr[iend] - base;
+  double *out = a.J + base;
+  for (int j = lane; j < total; j += 32) out[j] = buf[j];
 }
 
 // ---------------------------------------------------------------------------
@@ -496,6 +617,13 @@ int device_setup(_p_TDy *t) {
   UP(a.f_up, fup);
   UP(a.f_dn, fdn);
   UP(a.G, s.gravdis);
+  a.nC = s.nC;
+  a.nCpad = s.nCpad;
+  UP(a.Tc, s.Tc);
+  UP(a.cellc, s.cellc);
+  UP(a.facec, s.facec);
+  a.ngen = (int)s.gen_vertex.size();
+  UP(a.gen_vertex, s.gen_vertex);
   UP(a.v_row_off, s.v_row_off);
   UP(a.v_col_off, s.v_col_off);
   UP(a.v_nint, s.v_nint);
@@ -508,15 +636,19 @@ int device_setup(_p_TDy *t) {
   UP(a.trans, s.trans);
   UP(a.rowptr, s.rowptr);
   UP(a.cv_off, s.cv_off);
-  UP(a.cv_vertex, s.cv_vertex);
+  UP(a.cv_jbase, s.cv_jbase);
+  UP(a.cv_rbase, s.cv_rbase);
+  UP(a.cv_stride, s.cv_stride);
+  UP(a.cv_nint, s.cv_nint);
   UP(a.cv_local, s.cv_local);
   UP(a.cv_slot_off, s.cv_slot_off);
   UP(a.cv_slots, s.cv_slots);
+  a.max_row_nnz = s.max_row_nnz;
 #undef UP
   double *p;
   if ((ierr = dalloc(d, &a.P, next))) return ierr;
-  if ((ierr = dalloc(d, &a.rho, next))) return ierr;
-  if ((ierr = dalloc(d, &a.drho, next))) return ierr;
+  if ((ierr = dalloc(d, &a.hr, next))) return ierr;
+  if ((ierr = dalloc(d, &a.hdr, next))) return ierr;
   if ((ierr = dalloc(d, &a.lam, next))) return ierr;
   if ((ierr = dalloc(d, &a.dlam, next))) return ierr;
   if ((ierr = dalloc(d, &a.seep, next))) return ierr;
@@ -526,7 +658,7 @@ int device_setup(_p_TDy *t) {
   if ((ierr = dalloc(d, &p, m.nc))) return ierr;
   CUDA_TRY(cudaMemset(p, 0, sizeof(double) * m.nc));
   a.accum_prev = p;
-  if ((ierr = dalloc(d, &a.scratch, (size_t)s.v_jv_off[m.nv]))) return ierr;
+  if ((ierr = dalloc(d, &a.scratch, (size_t)s.scratch_size))) return ierr;
   d->nnz = (int)s.colidx.size();
   if ((ierr = dalloc(d, &d->dU, m.nc))) return ierr;
   if ((ierr = dalloc(d, &d->dUt, m.nc))) return ierr;
@@ -542,7 +674,7 @@ void device_destroy(_p_TDy *t) {
   DeviceState *d = t->dev;
   if (!d) return;
   if (d->stream) cudaStreamSynchronize(d->stream);
-  for (int k = 0; k < 4; k++)
+  for (int k = 0; k < 5; k++)
     if (d->ev[k]) cudaEventDestroy(d->ev[k]);
   for (void *p : d->allocs) cudaFree(p);
   if (d->stream) cudaStreamDestroy(d->stream);
@@ -577,6 +709,29 @@ int device_presolve_host(_p_TDy *t, const double *Uprev) {
   return 0;
 }
 
+// The four launches of one evaluation; events[] (5 entries, or null) bracket
+// them for the per-kernel timers.
+static int launch_eval(const DevArgs &a, cudaStream_t st, cudaEvent_t *events) {
+  const size_t canon_smem = 36 * 128 * sizeof(double);
+  const size_t cell_smem = 2 * 32 * (size_t)a.max_row_nnz * sizeof(double);
+  if (events) CUDA_TRY(cudaEventRecord(events[0], st));
+  state_kernel<<<nblocks(a.nc + a.nb, 256), 256, 0, st>>>(a);
+  if (events) CUDA_TRY(cudaEventRecord(events[1], st));
+  if (a.nC > 0) {
+    if (a.rho_type == WATER_DENSITY_EXPONENTIAL)
+      canon_vertex_kernel<false><<<nblocks(a.nC, 128), 128, canon_smem, st>>>(a);
+    else
+      canon_vertex_kernel<true><<<nblocks(a.nC, 128), 128, canon_smem, st>>>(a);
+  }
+  if (events) CUDA_TRY(cudaEventRecord(events[2], st));
+  if (a.ngen > 0) vertex_kernel<<<nblocks(a.ngen, 128), 128, 0, st>>>(a);
+  if (events) CUDA_TRY(cudaEventRecord(events[3], st));
+  cell_kernel<<<nblocks(a.nc, 64), 64, cell_smem, st>>>(a);
+  if (events) CUDA_TRY(cudaEventRecord(events[4], st));
+  CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
 int device_eval(_p_TDy *t, int form, double time, const double *dU, const double *dUt, double shift, double *dR,
                 double *dJ, void *stream) {
   (void)time;
@@ -594,17 +749,11 @@ int device_eval(_p_TDy *t, int form, double time, const double *dU, const double
   a.needJ = dJ != nullptr;
   a.R = dR;
   a.J = dJ;
-  if (d->timers) CUDA_TRY(cudaEventRecord(d->ev[0], st));
-  state_kernel<<<nblocks(a.nc + a.nb, 256), 256, 0, st>>>(a);
-  if (d->timers) CUDA_TRY(cudaEventRecord(d->ev[1], st));
-  vertex_kernel<<<nblocks(a.nv, 128), 128, 0, st>>>(a);
-  if (d->timers) CUDA_TRY(cudaEventRecord(d->ev[2], st));
-  cell_kernel<<<nblocks(a.nc, 128), 128, 0, st>>>(a);
-  if (d->timers) CUDA_TRY(cudaEventRecord(d->ev[3], st));
-  CUDA_TRY(cudaGetLastError());
+  int ierr = launch_eval(a, st, d->timers ? d->ev : nullptr);
+  if (ierr) return ierr;
   if (d->timers) {
-    CUDA_TRY(cudaEventSynchronize(d->ev[3]));
-    for (int k = 0; k < 3; k++) {
+    CUDA_TRY(cudaEventSynchronize(d->ev[4]));
+    for (int k = 0; k < 4; k++) {
       float ms = 0.f;
       CUDA_TRY(cudaEventElapsedTime(&ms, d->ev[k], d->ev[k + 1]));
       d->t_ms[k] += ms;
@@ -617,9 +766,9 @@ int device_eval(_p_TDy *t, int form, double time, const double *dU, const double
 int device_set_timers(_p_TDy *t, int on) {
   DeviceState *d = t->dev;
   if (on && !d->ev[0])
-    for (int k = 0; k < 4; k++) CUDA_TRY(cudaEventCreate(&d->ev[k]));
+    for (int k = 0; k < 5; k++) CUDA_TRY(cudaEventCreate(&d->ev[k]));
   d->timers = on != 0;
-  for (int k = 0; k < 3; k++) {
+  for (int k = 0; k < 4; k++) {
     d->t_ms[k] = 0.0;
     d->t_calls[k] = 0;
   }
@@ -629,8 +778,8 @@ int device_set_timers(_p_TDy *t, int on) {
 int device_get_timers(_p_TDy *t, int *n, const char **names, double *ms, long long *calls) {
   DeviceState *d = t->dev;
   int cap = *n;
-  *n = 3;
-  for (int k = 0; k < 3 && k < cap; k++) {
+  *n = 4;
+  for (int k = 0; k < 4 && k < cap; k++) {
     if (names) names[k] = kKernelNames[k];
     if (ms) ms[k] = d->t_ms[k];
     if (calls) calls[k] = d->t_calls[k];
@@ -723,7 +872,7 @@ static std::mutex g_noalloc_mutex;
 
 int device_eval_noalloc(_p_TDy *t, const double *dU, double *dR, double *dJ, void *stream) {
   DeviceState *d = t->dev;
-  const long long need = t->setup.v_jv_off[t->mesh.nv];
+  const long long need = t->setup.scratch_size;
   if (need > (long long)TDY_NOALLOC_SCRATCH_DOUBLES)
     return set_error(TDY_ERR_ARG_OUTOFRANGE,
                      "mesh needs %lld doubles of partial-sum scratch; the static scratch holds %llu (64 MiB). "
@@ -758,16 +907,12 @@ int device_eval_noalloc(_p_TDy *t, const double *dU, double *dR, double *dJ, voi
   a.R = dR;
   a.J = dJ;
   a.scratch = scratch;
-  state_kernel<<<nblocks(a.nc + a.nb, 256), 256, 0, st>>>(a);
-  vertex_kernel<<<nblocks(a.nv, 128), 128, 0, st>>>(a);
-  cell_kernel<<<nblocks(a.nc, 128), 128, 0, st>>>(a);
-  CUDA_TRY(cudaGetLastError());
-  return 0;
+  return launch_eval(a, st, nullptr);
 }
 
 int device_launches_per_eval(_p_TDy *t) {
-  (void)t;
-  return 3;
+  const DevArgs &a = t->dev->a;
+  return 2 + (a.nC > 0 ? 1 : 0) + (a.ngen > 0 ? 1 : 0);
 }
 
 int device_synchronize(_p_TDy *t) {

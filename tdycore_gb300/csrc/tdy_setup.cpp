@@ -281,7 +281,6 @@ int mpfao_setup(const Options &opt, const Mesh &m, const Materials &mat, const B
   s.v_col_off.assign(nv + 1, 0);
   s.v_nint.assign(nv, 0);
   s.v_trans_off.assign(nv + 1, 0);
-  s.v_jv_off.assign(nv + 1, 0);
 
   std::vector<int> fidx;  // face -> position at the current vertex (scratch)
   std::vector<int> fpos(m.nf, -1);
@@ -292,7 +291,6 @@ int mpfao_setup(const Options &opt, const Mesh &m, const Materials &mat, const B
       s.v_row_off[v + 1] = s.v_row_off[v];
       s.v_col_off[v + 1] = s.v_col_off[v];
       s.v_trans_off[v + 1] = s.v_trans_off[v];
-      s.v_jv_off[v + 1] = s.v_jv_off[v];
       continue;
     }
     // unknown / known numbering of the subfaces at v
@@ -377,7 +375,6 @@ int mpfao_setup(const Options &opt, const Mesh &m, const Materials &mat, const B
     s.v_row_off[v + 1] = s.v_row_off[v] + nrow;
     s.v_col_off[v + 1] = s.v_col_off[v] + ncol;
     s.v_trans_off[v + 1] = s.v_trans_off[v] + (long long)nrow * ncol;
-    s.v_jv_off[v + 1] = s.v_jv_off[v] + (long long)nint * nint + nint;
     for (int a = 0; a < nint; a++) s.col_ext.push_back(m.vert_cells[c0 + a]);
     for (int j = 0; j < nfv; j++)
       if (knw[j] >= 0) s.col_ext.push_back(nc + m.face_bnd[m.vert_faces[f0 + j]]);
@@ -452,6 +449,93 @@ int mpfao_setup(const Options &opt, const Mesh &m, const Materials &mat, const B
   }
   if (s.max_row_nnz > 255) return set_error(TDY_ERR_SUP, "Jacobian row with %d entries (max 255)", s.max_row_nnz);
 
+  // ---- canonical interior-hex vertices ----
+  std::vector<int> canon_idx(nv, -1);
+  std::vector<std::array<int, 8>> octant_col;  // octant -> vertex column, per canonical vertex
+  std::vector<std::array<int, 12>> canon_row;  // canonical row -> vertex row
+  for (int v = 0; v < nv; v++) {
+    const int nint = s.v_nint[v];
+    const int r0 = s.v_row_off[v], nrow = s.v_row_off[v + 1] - r0;
+    const int c0 = s.v_col_off[v], ncol = s.v_col_off[v + 1] - c0;
+    if (nint != 8 || nrow != 12 || ncol != 8) continue;
+    const double *xv = &m.vx[3 * (size_t)v];
+    std::array<int, 8> oc;
+    oc.fill(-1);
+    int oct_of[8];
+    bool ok = true;
+    for (int a = 0; a < 8 && ok; a++) {
+      const double *xc = &m.cell_cen[3 * (size_t)s.col_ext[c0 + a]];
+      int o = (xc[0] > xv[0] ? 1 : 0) | (xc[1] > xv[1] ? 2 : 0) | (xc[2] > xv[2] ? 4 : 0);
+      if (oc[o] >= 0) ok = false;
+      oc[o] = a;
+      oct_of[a] = o;
+    }
+    std::array<int, 12> cr;
+    cr.fill(-1);
+    for (int r = 0; r < nrow && ok; r++) {
+      int lu = s.row_lup[r0 + r], ld = s.row_ldn[r0 + r];
+      if (lu < 0 || ld < 0) {
+        ok = false;
+        break;
+      }
+      int ou = oct_of[lu], od = oct_of[ld];
+      int diff = ou ^ od;
+      if (diff != 1 && diff != 2 && diff != 4) {
+        ok = false;
+        break;
+      }
+      if (ou & diff) {  // the face's first cell must be on the lower side
+        ok = false;
+        break;
+      }
+      int k = (diff == 1) ? 0 : (diff == 2) ? 1 : 2;
+      int rc = -1;
+      for (int j = 0; j < 4; j++)
+        if (kCanonUp[4 * k + j] == ou) rc = 4 * k + j;
+      if (rc < 0 || cr[rc] >= 0) {
+        ok = false;
+        break;
+      }
+      cr[rc] = r;
+    }
+    if (!ok) continue;
+    canon_idx[v] = (int)s.canon_vertex.size();
+    s.canon_vertex.push_back(v);
+    octant_col.push_back(oc);
+    canon_row.push_back(cr);
+  }
+  s.nC = (int)s.canon_vertex.size();
+  s.nCpad = ((s.nC + 31) / 32) * 32;
+  const long long P = s.nCpad;
+  s.Tc.assign(96 * (size_t)P, 0.0);
+  s.cellc.assign(8 * (size_t)P, 0);
+  s.facec.assign(12 * (size_t)P, 0);
+  for (int k = 0; k < s.nC; k++) {
+    const int v = s.canon_vertex[k];
+    const int r0 = s.v_row_off[v], c0 = s.v_col_off[v];
+    const double *T = &s.trans[s.v_trans_off[v]];
+    for (int o = 0; o < 8; o++) s.cellc[o * P + k] = s.col_ext[c0 + octant_col[k][o]];
+    for (int rc = 0; rc < 12; rc++) {
+      const int r = canon_row[k][rc];
+      s.facec[rc * P + k] = s.row_face[r0 + r];
+      for (int o = 0; o < 8; o++) s.Tc[(rc * 8 + o) * P + k] = T[r * 8 + octant_col[k][o]];
+    }
+  }
+  // scratch layout
+  s.v_jv_off.assign(nv, -1);
+  long long off = 72 * P;
+  for (int v = 0; v < nv; v++) {
+    if (s.v_nint[v] == 0) continue;
+    if (canon_idx[v] >= 0) {
+      s.v_jv_off[v] = canon_idx[v];
+    } else {
+      s.gen_vertex.push_back(v);
+      s.v_jv_off[v] = off;
+      off += (long long)s.v_nint[v] * s.v_nint[v] + s.v_nint[v];
+    }
+  }
+  s.scratch_size = off;
+
   // ---- cell gather program ----
   s.cv_off.assign(nc + 1, 0);
   for (int c = 0; c < nc; c++) {
@@ -459,20 +543,35 @@ int mpfao_setup(const Options &opt, const Mesh &m, const Materials &mat, const B
     const int rn = s.rowptr[c + 1] - s.rowptr[c];
     for (int j = m.cell_vert_off[c]; j < m.cell_vert_off[c + 1]; j++) {
       int v = m.cell_verts[j];
-      int k0 = m.vert_cell_off[v], nint = m.vert_cell_off[v + 1] - k0;
+      const int c0 = s.v_col_off[v], nint = s.v_nint[v];
+      std::vector<int> cols(nint);
+      if (canon_idx[v] >= 0) {
+        for (int o = 0; o < 8; o++) cols[o] = s.col_ext[c0 + octant_col[canon_idx[v]][o]];
+      } else {
+        for (int k = 0; k < nint; k++) cols[k] = s.col_ext[c0 + k];
+      }
       int a = -1;
       for (int k = 0; k < nint; k++)
-        if (m.vert_cells[k0 + k] == c) a = k;
-      s.cv_vertex.push_back(v);
+        if (cols[k] == c) a = k;
+      if (a < 0) return set_error(TDY_ERR_LIB, "cell %d missing at its vertex %d", c, v);
+      if (canon_idx[v] >= 0) {
+        s.cv_jbase.push_back((long long)(a * 8) * P + canon_idx[v]);
+        s.cv_rbase.push_back((long long)(64 + a) * P + canon_idx[v]);
+        s.cv_stride.push_back((int)P);
+      } else {
+        s.cv_jbase.push_back(s.v_jv_off[v] + (long long)a * nint);
+        s.cv_rbase.push_back(s.v_jv_off[v] + (long long)nint * nint + a);
+        s.cv_stride.push_back(1);
+      }
+      s.cv_nint.push_back(nint);
       s.cv_local.push_back(a);
       s.cv_slot_off.push_back((int)s.cv_slots.size());
       for (int k = 0; k < nint; k++) {
-        int col = m.vert_cells[k0 + k];
-        int pos = (int)(std::lower_bound(row, row + rn, col) - row);
+        int pos = (int)(std::lower_bound(row, row + rn, cols[k]) - row);
         s.cv_slots.push_back((uint8_t)pos);
       }
     }
-    s.cv_off[c + 1] = (int)s.cv_vertex.size();
+    s.cv_off[c + 1] = (int)s.cv_jbase.size();
   }
   return 0;
 }
