@@ -362,16 +362,17 @@ __global__ void __launch_bounds__(128) canon_vertex_kernel(DevArgs a) {
   for (int r = 0; r < 12; r++) {
     const int u = canon_up(r), d = canon_dn(r);
     const double *T = a.Tc + (long long)(r * 8) * P + vc;
-    double TP = 0.0;
+    // explicit roundings: the same bits whichever outputs a call requests
+    double TP = __dmul_rn(T[0], p[0]);
 #pragma unroll
-    for (int c = 0; c < 8; c++) TP += T[c * P] * p[c];
+    for (int c = 1; c < 8; c++) TP = __fma_rn(T[c * P], p[c], TP);
     const double G = a.G[a.facec[r * P + vc]];
-    const double den = hr[u] + hr[d];
-    const double q = TP + den * G;
+    const double den = __dadd_rn(hr[u], hr[d]);
+    const double q = __fma_rn(den, G, TP);
     const bool fdn = q < 0.0;
     const double lm = fdn ? lam[u] : lam[d];
-    const double w = den * lm;
-    const double flux = -(w * q);
+    const double w = __dmul_rn(den, lm);
+    const double flux = -__dmul_rn(w, q);
     Rv[u] += flux;
     Rv[d] -= flux;
     if (a.needJ) {
@@ -443,18 +444,18 @@ __global__ void __launch_bounds__(128) vertex_kernel(DevArgs a) {
   for (int r = 0; r < nrow; r++) {
     const double *Tr = T + (size_t)r * ncol;
     double TP = 0.0;
-    for (int c = 0; c < ncol; c++) TP += Tr[c] * a.P[a.col_ext[c0 + c]];
+    for (int c = 0; c < ncol; c++) TP = __fma_rn(Tr[c], a.P[a.col_ext[c0 + c]], TP);
     const int f = a.row_face[r0 + r];
     const int up = a.f_up[f], dn = a.f_dn[f];
     const double G = a.G[f];
-    const double den = a.hr[up] + a.hr[dn];
-    const double q = TP + den * G;
+    const double den = __dadd_rn(a.hr[up], a.hr[dn]);
+    const double q = __fma_rn(den, G, TP);
     const bool flowdn = q < 0.0;
     const int u = flowdn ? up : dn;
     const double lm = a.lam[u];
     const bool zero = a.seep[u] != 0;
-    const double wr = zero ? 0.0 : den * lm;
-    fl[r] = -(wr * q);
+    const double wr = zero ? 0.0 : __dmul_rn(den, lm);
+    fl[r] = -__dmul_rn(wr, q);
     if (a.needJ) {
       w[r] = wr;
       if (zero) {
