@@ -146,6 +146,13 @@ struct MPFAOSetup {
   std::vector<int> cv_local;       // a: local index of the cell at the vertex
   std::vector<int> cv_slot_off;    // offset into cv_slots for this (cell, vertex)
   std::vector<uint8_t> cv_slots;   // CSR slot (within the row) of each vertex column
+  // Structured interior cells: all 8 vertices canonical, 27-entry row in
+  // (dz, dy, dx) order, vertices in corner order (see kCornerOffset).  Their
+  // gather needs only the 8 canonical vertex indices (SoA, stride nSpad).
+  int nS = 0, nSpad = 0;
+  std::vector<int> sc_cells;       // nS
+  std::vector<int> sc_vc;          // 8 * nSpad
+  std::vector<int> gc_cells;       // the other cells
   int max_nint = 0, max_nrow = 0, max_ncol = 0, max_row_nnz = 0;
 };
 
@@ -155,6 +162,18 @@ int mpfao_setup(const Options &opt, const Mesh &m, const Materials &mat, const B
 // side, the face's first cell) and kCanonDn[r] = kCanonUp[r] | (1 << (r / 4)).
 constexpr int kCanonUp[12] = {0, 2, 4, 6, 0, 1, 4, 5, 0, 1, 2, 3};
 constexpr int kCanonDn[12] = {1, 3, 5, 7, 2, 3, 6, 7, 4, 5, 6, 7};
+
+// Hexahedron corner j (bottom face counter-clockwise, then top face) at
+// offset (x, y, z) in {0,1}^3 from the cell's lowest corner; the cell lies in
+// octant struct_octant(j) of that vertex, and octant b of that vertex holds
+// the neighbour whose slot in a 27-entry (dz, dy, dx)-ordered row is
+// struct_slot(j, b).
+constexpr int kCornerOffset[8] = {0, 1, 3, 2, 4, 5, 7, 6};  // bit0 x, bit1 y, bit2 z
+inline constexpr int struct_octant(int j) { return 7 ^ kCornerOffset[j]; }
+inline constexpr int struct_slot(int j, int b) {
+  return ((((kCornerOffset[j] >> 2) & 1) - 1 + ((b >> 2) & 1)) + 1) * 9 +
+         ((((kCornerOffset[j] >> 1) & 1) - 1 + ((b >> 1) & 1)) + 1) * 3 + (((kCornerOffset[j] & 1) - 1 + (b & 1)) + 1);
+}
 
 // EOS at one pressure (src/materials/tdyeos.c:5-136).
 void eos_density(int type, double p, double *rho, double *drho, double *d2rho);

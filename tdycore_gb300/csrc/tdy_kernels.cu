@@ -1,7 +1,7 @@
 // tdy_kernels.cu -- sm_103a kernels of the MPFA-O Richards residual and
 // Jacobian, and their host-side launch code.
 //
-// One evaluation is four launches on one stream:
+// One evaluation is three launches on one stream:
 //   1. state_kernel   (cells, then boundary faces)
 //        TDyUpdateState_Richards_MPFAO (src/fv/mpfao/tdympfao.c:2527-2594),
 //        TDyMPFAO_SetBoundaryPressure + TDyMPFAOUpdateBoundaryState
@@ -9,8 +9,8 @@
 //        terms of TDyMPFAOSNESFunction/Jacobian (tdympfao_snes.c:19-30,
 //        112-123, 166-179) or TDyMPFAOIFunction/IJacobian_Accumulation
 //        (tdympfao_ts.c:191-212, 459-517).
-//   2. canon_vertex_kernel  (one thread per interior hexahedral vertex)
-//   3. vertex_kernel        (one thread per other vertex)
+//   2. vertex_kernel  (one thread per vertex; interior hexahedral vertices
+//                      first, in their own blocks, then the others)
 //        MatMult(Trans_mat, P_vec) (tdympfao_ts.c:184) restricted to the
 //        vertex's rows, the upwinded flux of TDyMPFAOIFunction_Vertices
 //        (tdympfao_ts.c:12-150) and the Jacobian entries of
@@ -21,7 +21,7 @@
 //        octant layout (rows and columns known at compile time, structure-of-
 //        arrays storage read with coalesced loads); the rest use per-vertex
 //        blocks.
-//   4. cell_kernel    (one thread per cell)
+//   3. cell_kernel    (one thread per cell)
 //        sums, in a fixed order, the partials of the cell's vertices into
 //        R[cell] and into the cell's row of the fixed CSR pattern, then adds
 //        the accumulation terms.  No atomics: results are bitwise
@@ -87,20 +87,22 @@ struct DevArgs {
   const long long *cv_jbase, *cv_rbase;
   const unsigned char *cv_slots;
   int max_row_nnz;
+  int nS, nSpad, ngc;
+  const int *sc_cells, *sc_vc, *gc_cells;
   // outputs
   double *R, *J;
 };
 
-static const char *const kKernelNames[4] = {"state_kernel", "canon_vertex_kernel", "vertex_kernel", "cell_kernel"};
+static const char *const kKernelNames[3] = {"state_kernel", "vertex_kernel", "cell_kernel"};
 
 struct DeviceState {
   cudaStream_t stream = nullptr;
   DevArgs a;
   // per-kernel timers (TDY_START_FUNCTION_TIMER analogue, include/tdytimers.h)
   bool timers = false;
-  cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-  double t_ms[4] = {0, 0, 0, 0};
-  long long t_calls[4] = {0, 0, 0, 0};
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  double t_ms[3] = {0, 0, 0};
+  long long t_calls[3] = {0, 0, 0};
   int device = 0;  // CUDA device current at TDySetup
   // owned allocations
   std::vector<void *> allocs;
@@ -331,6 +333,19 @@ static_assert(canon_up(5) == kCanonUp[5] && canon_dn(5) == kCanonDn[5] && canon_
                   canon_dn(10) == kCanonDn[10] && canon_up(2) == kCanonUp[2] && canon_dn(7) == kCanonDn[7],
               "canonical row tables disagree");
 
+// Corner offsets, octants and slots of structured cells (kCornerOffset,
+// struct_octant, struct_slot in tdy_internal.h) without host tables.
+__host__ __device__ constexpr int corner_offset(int j) { return j ^ ((j >> 1) & 1); }
+__host__ __device__ constexpr int d_struct_octant(int j) { return 7 ^ corner_offset(j); }
+__host__ __device__ constexpr int d_struct_slot(int j, int b) {
+  return ((((corner_offset(j) >> 2) & 1) - 1 + ((b >> 2) & 1)) + 1) * 9 +
+         ((((corner_offset(j) >> 1) & 1) - 1 + ((b >> 1) & 1)) + 1) * 3 + (((corner_offset(j) & 1) - 1 + (b & 1)) + 1);
+}
+static_assert(corner_offset(2) == kCornerOffset[2] && corner_offset(7) == kCornerOffset[7] &&
+                  d_struct_slot(0, 7) == struct_slot(0, 7) && d_struct_slot(6, 0) == struct_slot(6, 0) &&
+                  d_struct_slot(3, 5) == struct_slot(3, 5),
+              "structured-cell tables disagree");
+
 // Row of the canonical layout that joins octant c with its neighbour across
 // axis k, and whether c is that row's first ("up") cell.
 __host__ __device__ constexpr int canon_row(int c, int k) {
@@ -339,10 +354,10 @@ __host__ __device__ constexpr int canon_row(int c, int k) {
 __host__ __device__ constexpr bool canon_is_up(int c, int k) { return ((c >> k) & 1) == 0; }
 
 template <bool CONST_RHO>
-__global__ void __launch_bounds__(128) canon_vertex_kernel(DevArgs a) {
+__device__ __forceinline__ void canon_vertex(const DevArgs &a, int block) {
   extern __shared__ double sh[];  // [36][blockDim]: w, E_up, E_dn per row
   const int tid = threadIdx.x, bs = blockDim.x;
-  const int vc = blockIdx.x * bs + tid;
+  const int vc = block * bs + tid;
   if (vc >= a.nC) return;
   const long long P = a.nCpad;
   double p[8], hr[8], lam[8], dlam[8], hdr[8];
@@ -429,8 +444,8 @@ __global__ void __launch_bounds__(128) canon_vertex_kernel(DevArgs a) {
 
 // ---------------------------------------------------------------------------
 // 3. other vertices: per-vertex blocks
-__global__ void __launch_bounds__(128) vertex_kernel(DevArgs a) {
-  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void generic_vertex(const DevArgs &a, int block) {
+  const int g = block * blockDim.x + threadIdx.x;
   if (g >= a.ngen) return;
   const int v = a.gen_vertex[g];
   const int nint = a.v_nint[v];
@@ -496,17 +511,65 @@ __global__ void __launch_bounds__(128) vertex_kernel(DevArgs a) {
   }
 }
 
+// Canonical vertices take the first blocks of the launch, the others the rest.
+template <bool CONST_RHO>
+__global__ void __launch_bounds__(128) vertex_kernel(DevArgs a, int canon_blocks) {
+  if ((int)blockIdx.x < canon_blocks)
+    canon_vertex<CONST_RHO>(a, blockIdx.x);
+  else
+    generic_vertex(a, blockIdx.x - canon_blocks);
+}
+
 // ---------------------------------------------------------------------------
-// 4. per-cell deterministic gather into R and the CSR row.  Each warp stages
-// its 32 consecutive rows (contiguous in the CSR value array) in shared memory
-// and writes them out with coalesced stores.
-__global__ void __launch_bounds__(64) cell_kernel(DevArgs a) {
+// 4. per-cell deterministic gather into R and the CSR row.
+//
+// Structured interior cells (all vertices canonical, 27-point row) read their
+// eight vertices' partials at compile-time slots.  Other cells follow their
+// gather program; each warp stages its rows in shared memory and writes them
+// with coalesced stores.  Both sum the vertices in the cell's corner order, so
+// a cell gets the same bits on either path.
+__device__ __forceinline__ void struct_cell(const DevArgs &a, int block) {
+  const int sidx = block * blockDim.x + threadIdx.x;
+  if (sidx >= a.nS) return;
+  const int i = a.sc_cells[sidx];
+  const long long P = a.nCpad, Q = a.nSpad;
+  int vc[8];
+#pragma unroll
+  for (int j = 0; j < 8; j++) vc[j] = a.sc_vc[j * Q + sidx];
+  const double *S = a.scratch;
+  if (a.needR) {
+    double s = 0.0;
+#pragma unroll
+    for (int j = 0; j < 8; j++) s += S[(64 + d_struct_octant(j)) * P + vc[j]];
+    s += a.acc_a[i];
+    s -= a.acc_b[i];
+    a.R[i] = s;
+  }
+  if (a.needJ) {
+    double row[27];
+#pragma unroll
+    for (int k = 0; k < 27; k++) row[k] = 0.0;
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      const double *blk = S + (long long)(d_struct_octant(j) * 8) * P + vc[j];
+#pragma unroll
+      for (int b = 0; b < 8; b++) row[d_struct_slot(j, b)] += blk[b * P];
+    }
+    row[13] += a.jdiag[i];
+    double *out = a.J + a.rowptr[i];
+#pragma unroll
+    for (int k = 0; k < 27; k++) out[k] = row[k];
+  }
+}
+
+__device__ __forceinline__ void generic_cell(const DevArgs &a, int block) {
   extern __shared__ double rowbuf[];  // [warps][32 * max_row_nnz]
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int gidx = block * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int i0 = i - lane;
-  if (i0 >= a.nc) return;  // whole warp out of range
-  const bool active = i < a.nc;
+  const int g0 = gidx - lane;
+  if (g0 >= a.ngc) return;  // whole warp out of range
+  const bool active = gidx < a.ngc;
+  const int i = active ? a.gc_cells[gidx] : -1;
   if (a.needR && active) {
     const int k0 = a.cv_off[i], k1 = a.cv_off[i + 1];
     double s = 0.0;
@@ -516,12 +579,11 @@ __global__ void __launch_bounds__(64) cell_kernel(DevArgs a) {
     a.R[i] = s;
   }
   if (!a.needJ) return;
-  const int iend = min(i0 + 32, a.nc);
-  const int base = a.rowptr[i0];
-  double *buf = rowbuf + (size_t)warp * 32 * a.max_row_nnz;
+  double *row = rowbuf + ((size_t)warp * 32 + lane) * a.max_row_nnz;
+  int p0 = 0, rn = 0;
   if (active) {
-    const int p0 = a.rowptr[i], rn = a.rowptr[i + 1] - p0;
-    double *row = buf + (p0 - base);
+    p0 = a.rowptr[i];
+    rn = a.rowptr[i + 1] - p0;
     for (int j = 0; j < rn; j++) row[j] = 0.0;
     const int k0 = a.cv_off[i], k1 = a.cv_off[i + 1];
     int diag = -1;
@@ -533,11 +595,16 @@ __global__ void __launch_bounds__(64) cell_kernel(DevArgs a) {
       diag = sl[a.cv_local[k]];
     }
     if (diag >= 0) row[diag] += a.jdiag[i];
+    double *out = a.J + p0;
+    for (int j = 0; j < rn; j++) out[j] = row[j];
   }
-  __syncwarp();
-  const int total = a.rowptr[iend] - base;
-  double *out = a.J + base;
-  for (int j = lane; j < total; j += 32) out[j] = buf[j];
+}
+
+__global__ void __launch_bounds__(64) cell_kernel(DevArgs a, int struct_blocks) {
+  if ((int)blockIdx.x < struct_blocks)
+    struct_cell(a, blockIdx.x);
+  else
+    generic_cell(a, blockIdx.x - struct_blocks);
 }
 
 // ---------------------------------------------------------------------------
@@ -645,6 +712,12 @@ int device_setup(_p_TDy *t) {
   UP(a.cv_slot_off, s.cv_slot_off);
   UP(a.cv_slots, s.cv_slots);
   a.max_row_nnz = s.max_row_nnz;
+  a.nS = s.nS;
+  a.nSpad = s.nSpad;
+  a.ngc = (int)s.gc_cells.size();
+  UP(a.sc_cells, s.sc_cells);
+  UP(a.sc_vc, s.sc_vc);
+  UP(a.gc_cells, s.gc_cells);
 #undef UP
   double *p;
   if ((ierr = dalloc(d, &a.P, next))) return ierr;
@@ -675,7 +748,7 @@ void device_destroy(_p_TDy *t) {
   DeviceState *d = t->dev;
   if (!d) return;
   if (d->stream) cudaStreamSynchronize(d->stream);
-  for (int k = 0; k < 5; k++)
+  for (int k = 0; k < 4; k++)
     if (d->ev[k]) cudaEventDestroy(d->ev[k]);
   for (void *p : d->allocs) cudaFree(p);
   if (d->stream) cudaStreamDestroy(d->stream);
@@ -714,21 +787,21 @@ int device_presolve_host(_p_TDy *t, const double *Uprev) {
 // them for the per-kernel timers.
 static int launch_eval(const DevArgs &a, cudaStream_t st, cudaEvent_t *events) {
   const size_t canon_smem = 36 * 128 * sizeof(double);
-  const size_t cell_smem = 2 * 32 * (size_t)a.max_row_nnz * sizeof(double);
+  const size_t cell_smem = 64 * (size_t)a.max_row_nnz * sizeof(double);
+  const int cb = (int)nblocks(a.nC, 128), gb = (int)nblocks(a.ngen, 128);
+  const int sb = (int)nblocks(a.nS, 64), gcb = (int)nblocks(a.ngc, 64);
   if (events) CUDA_TRY(cudaEventRecord(events[0], st));
   state_kernel<<<nblocks(a.nc + a.nb, 256), 256, 0, st>>>(a);
   if (events) CUDA_TRY(cudaEventRecord(events[1], st));
-  if (a.nC > 0) {
+  if (cb + gb > 0) {
     if (a.rho_type == WATER_DENSITY_EXPONENTIAL)
-      canon_vertex_kernel<false><<<nblocks(a.nC, 128), 128, canon_smem, st>>>(a);
+      vertex_kernel<false><<<cb + gb, 128, canon_smem, st>>>(a, cb);
     else
-      canon_vertex_kernel<true><<<nblocks(a.nC, 128), 128, canon_smem, st>>>(a);
+      vertex_kernel<true><<<cb + gb, 128, canon_smem, st>>>(a, cb);
   }
   if (events) CUDA_TRY(cudaEventRecord(events[2], st));
-  if (a.ngen > 0) vertex_kernel<<<nblocks(a.ngen, 128), 128, 0, st>>>(a);
+  if (sb + gcb > 0) cell_kernel<<<sb + gcb, 64, cell_smem, st>>>(a, sb);
   if (events) CUDA_TRY(cudaEventRecord(events[3], st));
-  cell_kernel<<<nblocks(a.nc, 64), 64, cell_smem, st>>>(a);
-  if (events) CUDA_TRY(cudaEventRecord(events[4], st));
   CUDA_TRY(cudaGetLastError());
   return 0;
 }
@@ -753,8 +826,8 @@ int device_eval(_p_TDy *t, int form, double time, const double *dU, const double
   int ierr = launch_eval(a, st, d->timers ? d->ev : nullptr);
   if (ierr) return ierr;
   if (d->timers) {
-    CUDA_TRY(cudaEventSynchronize(d->ev[4]));
-    for (int k = 0; k < 4; k++) {
+    CUDA_TRY(cudaEventSynchronize(d->ev[3]));
+    for (int k = 0; k < 3; k++) {
       float ms = 0.f;
       CUDA_TRY(cudaEventElapsedTime(&ms, d->ev[k], d->ev[k + 1]));
       d->t_ms[k] += ms;
@@ -767,9 +840,9 @@ int device_eval(_p_TDy *t, int form, double time, const double *dU, const double
 int device_set_timers(_p_TDy *t, int on) {
   DeviceState *d = t->dev;
   if (on && !d->ev[0])
-    for (int k = 0; k < 5; k++) CUDA_TRY(cudaEventCreate(&d->ev[k]));
+    for (int k = 0; k < 4; k++) CUDA_TRY(cudaEventCreate(&d->ev[k]));
   d->timers = on != 0;
-  for (int k = 0; k < 4; k++) {
+  for (int k = 0; k < 3; k++) {
     d->t_ms[k] = 0.0;
     d->t_calls[k] = 0;
   }
@@ -779,8 +852,8 @@ int device_set_timers(_p_TDy *t, int on) {
 int device_get_timers(_p_TDy *t, int *n, const char **names, double *ms, long long *calls) {
   DeviceState *d = t->dev;
   int cap = *n;
-  *n = 4;
-  for (int k = 0; k < 4 && k < cap; k++) {
+  *n = 3;
+  for (int k = 0; k < 3 && k < cap; k++) {
     if (names) names[k] = kKernelNames[k];
     if (ms) ms[k] = d->t_ms[k];
     if (calls) calls[k] = d->t_calls[k];
@@ -913,7 +986,7 @@ int device_eval_noalloc(_p_TDy *t, const double *dU, double *dR, double *dJ, voi
 
 int device_launches_per_eval(_p_TDy *t) {
   const DevArgs &a = t->dev->a;
-  return 2 + (a.nC > 0 ? 1 : 0) + (a.ngen > 0 ? 1 : 0);
+  return 1 + ((a.nC + a.ngen) > 0 ? 1 : 0) + ((a.nS + a.ngc) > 0 ? 1 : 0);
 }
 
 int device_synchronize(_p_TDy *t) {

@@ -573,6 +573,35 @@ int mpfao_setup(const Options &opt, const Mesh &m, const Materials &mat, const B
     }
     s.cv_off[c + 1] = (int)s.cv_jbase.size();
   }
+
+  // ---- structured interior cells ----
+  std::vector<std::array<int, 8>> svc;
+  for (int c = 0; c < nc; c++) {
+    bool ok = (s.rowptr[c + 1] - s.rowptr[c] == 27) && (s.cv_off[c + 1] - s.cv_off[c] == 8);
+    std::array<int, 8> vcs;
+    for (int j = 0; ok && j < 8; j++) {
+      const int k = s.cv_off[c] + j;
+      const int v = m.cell_verts[m.cell_vert_off[c] + j];
+      if (canon_idx[v] < 0 || s.cv_local[k] != struct_octant(j)) {
+        ok = false;
+        break;
+      }
+      for (int b = 0; b < 8; b++)
+        if (s.cv_slots[s.cv_slot_off[k] + b] != struct_slot(j, b)) ok = false;
+      vcs[j] = canon_idx[v];
+    }
+    if (ok) {
+      s.sc_cells.push_back(c);
+      svc.push_back(vcs);
+    } else {
+      s.gc_cells.push_back(c);
+    }
+  }
+  s.nS = (int)s.sc_cells.size();
+  s.nSpad = ((s.nS + 31) / 32) * 32;
+  s.sc_vc.assign(8 * (size_t)s.nSpad, 0);
+  for (int k = 0; k < s.nS; k++)
+    for (int j = 0; j < 8; j++) s.sc_vc[(size_t)j * s.nSpad + k] = svc[k][j];
   return 0;
 }
 
