@@ -617,6 +617,22 @@ static int build_materials(TDy t) {
     mat.relperm_type[c] = REL_PERM_FUNC_IRMAY;
     mat.relperm_param[9 * (size_t)c] = ov.second;
   }
+  // Saturated-cell mobility kr(Se = 1)/mu, evaluated with the reference's
+  // expressions (tdycharacteristiccurves.c:451-460, 551-562, 607-614).
+  {
+    double d1, d2;
+    eos_viscosity(o.mu_type, o.Pref, &mat.vis, &d1, &d2);
+    mat.lam_sat.assign(nc, 0.0);
+    for (int c = 0; c < nc; c++) {
+      const double *rp = &mat.relperm_param[9 * (size_t)c];
+      double Kr = 1.0;
+      if (mat.relperm_type[c] == REL_PERM_FUNC_MUALEM && 1.0 > rp[2]) {
+        double xt = (1.0 - rp[1]) / rp[4];
+        Kr = rp[5] + xt * (rp[6] + xt * (rp[7] + xt * rp[8]));
+      }
+      mat.lam_sat[c] = Kr / mat.vis;
+    }
+  }
   mat.source_sink.assign(nc, 0.0);
   for (auto &ov : t->source_over) {
     if (ov.first < 0 || ov.first >= nc) return set_error(TDY_ERR_ARG_OUTOFRANGE, "cell %d out of range", ov.first);

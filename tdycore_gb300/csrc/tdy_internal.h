@@ -99,6 +99,8 @@ struct Materials {
   std::vector<int> relperm_type;   // nc
   std::vector<double> relperm_param;  // 9*nc
   std::vector<double> source_sink; // nc
+  std::vector<double> lam_sat;     // nc: kr(Se = 1) / mu
+  double vis = 0.0;                // water viscosity (pressure independent)
 };
 
 // Per-boundary-face condition data.
@@ -133,7 +135,8 @@ struct MPFAOSetup {
   std::vector<int> cellc;          // 8 * nCpad
   std::vector<int> facec;          // 12 * nCpad
   std::vector<int> gen_vertex;     // other vertices with cells (generic path)
-  // Scratch: canonical partials SoA [72][nCpad] (J_v row-major then R_v),
+  // Scratch: canonical partials, J_v as [octant][nCpad][8] then R_v as
+  // [octant][nCpad],
   // then generic per-vertex blocks J_v[nint][nint], R_v[nint].
   std::vector<long long> v_jv_off; // nv: generic block offset, or canonical column index
   long long scratch_size = 0;

@@ -58,6 +58,8 @@ struct DevArgs {
   const double *U, *Ut;
   // cells
   const double *vol, *poro, *Sr, *sat_param, *rp_param, *ss, *accum_prev;
+  const double *lam_sat;  // kr(Se = 1) / mu per cell (saturated cells)
+  double vis;             // water viscosity (constant at Tref and zero salinity)
   const int *sat_type, *rp_type;
   // boundary faces
   const int *bnd_cell, *bnd_type, *bnd_has;
@@ -237,33 +239,48 @@ __global__ void __launch_bounds__(256) state_kernel(DevArgs a) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < a.nc) {
     const double U = a.U[i];
-    const double Sr = a.Sr[i];
     const double Pc = a.Pref - U;
-    double S, dS, d2S;
-    saturation(a.sat_type[i], a.sat_param + 3 * (size_t)i, Sr, Pc, &S, &dS, &d2S);
-    double Se = (S - Sr) / (1.0 - Sr);
-    double Kr, dKr_dSe;
-    relperm(a.rp_type[i], a.rp_param + 9 * (size_t)i, Se, &Kr, &dKr_dSe);
-    double dSe_dS = 1.0 / (1.0 - Sr);
-    double dKr_dS = dKr_dSe * dSe_dS;
-    double P = a.Pref - Pc;
-    double rho, drho, d2rho, vis, dvis;
+    const double P = a.Pref - Pc;
+    const int st = a.sat_type[i];
+    // Saturated cells (van Genuchten Pc <= 0, Gardner Pc < 0): S = 1, dS = 0,
+    // Se = (1 - Sr)/(1 - Sr) = 1 exactly, so kr/mu is the per-cell constant
+    // lam_sat and its pressure derivative is zero.
+    const bool saturated = (st == SAT_FUNC_VAN_GENUCHTEN) ? (Pc <= 0) : (Pc < 0);
+    double S, dS, d2S, lam, dlam;
+    if (saturated) {
+      S = 1.0;
+      dS = 0.0;
+      d2S = 0.0;
+      lam = a.lam_sat[i];
+      dlam = 0.0;
+    } else {
+      const double Sr = a.Sr[i];
+      saturation(st, a.sat_param + 3 * (size_t)i, Sr, Pc, &S, &dS, &d2S);
+      double Se = (S - Sr) / (1.0 - Sr);
+      double Kr, dKr_dSe;
+      relperm(a.rp_type[i], a.rp_param + 9 * (size_t)i, Se, &Kr, &dKr_dSe);
+      double dSe_dS = 1.0 / (1.0 - Sr);
+      double dKr_dS = dKr_dSe * dSe_dS;
+      lam = Kr / a.vis;
+      dlam = dKr_dS * dS / a.vis;  // the viscosity does not depend on pressure here
+    }
+    double rho, drho, d2rho;
     density(a.rho_type, P, &rho, &drho, &d2rho);
-    viscosity(a.mu_type, &vis, &dvis);
     a.P[i] = P;
     a.hr[i] = 0.5 * rho;
     a.hdr[i] = 0.5 * drho;
-    a.lam[i] = Kr / vis;
-    a.dlam[i] = dKr_dS * dS / vis - Kr / (vis * vis) * dvis;
+    a.lam[i] = lam;
+    a.dlam[i] = dlam;
     a.seep[i] = 0;
     const double poro = a.poro[i], vol = a.vol[i];
     const double dporo = 0.0;
     double dmass = rho * dporo * S + drho * poro * S + rho * poro * dS;
     if (a.form == FORM_SNES) {
-      double acc = rho * poro * S * vol / a.dt;
+      const double dtInv = a.shift;  // 1/dt, computed on the host
+      double acc = rho * poro * S * vol * dtInv;
       a.acc_a[i] = acc - a.accum_prev[i];
       a.acc_b[i] = a.ss[i];
-      a.jdiag[i] = dmass * vol * (1.0 / a.dt);
+      a.jdiag[i] = dmass * vol * dtInv;
     } else {
       const double Ut = a.Ut[i];
       const double d2poro = 0.0;
@@ -277,16 +294,25 @@ __global__ void __launch_bounds__(256) state_kernel(DevArgs a) {
     const int b = i - a.nc;
     const int c = a.bnd_cell[b];
     const double p = a.bnd_has[b] ? a.bnd_val[b] : a.U[c];
-    const double Sr = a.Sr[c];
-    double S, dS, d2S;
-    saturation(a.sat_type[c], a.sat_param + 3 * (size_t)c, Sr, a.Pref - p, &S, &dS, &d2S);
-    double Se = (S - Sr) / (1.0 - Sr);
-    double Kr, dKr;
-    relperm(a.rp_type[c], a.rp_param + 9 * (size_t)c, Se, &Kr, &dKr);
+    const double Pc = a.Pref - p;
+    const int st = a.sat_type[c];
+    const bool saturated = (st == SAT_FUNC_VAN_GENUCHTEN) ? (Pc <= 0) : (Pc < 0);
+    double lam;
+    if (saturated) {
+      lam = a.lam_sat[c];  // kr(1) / mu with the boundary viscosity (the same constant)
+    } else {
+      const double Sr = a.Sr[c];
+      double S, dS, d2S;
+      saturation(st, a.sat_param + 3 * (size_t)c, Sr, Pc, &S, &dS, &d2S);
+      double Se = (S - Sr) / (1.0 - Sr);
+      double Kr, dKr;
+      relperm(a.rp_type[c], a.rp_param + 9 * (size_t)c, Se, &Kr, &dKr);
+      lam = Kr / a.bnd_vis[b];
+    }
     a.P[i] = p;
     a.hr[i] = 0.5 * a.bnd_rho[b];
     a.hdr[i] = 0.0;
-    a.lam[i] = Kr / a.bnd_vis[b];
+    a.lam[i] = lam;
     a.dlam[i] = 0.0;
     a.seep[i] = (a.bnd_type[b] == SEEPAGE_BC && p <= a.Pref) ? 1 : 0;
   }
@@ -409,7 +435,7 @@ __device__ __forceinline__ void canon_vertex(const DevArgs &a, int block) {
   double *S = a.scratch;
   if (a.needR) {
 #pragma unroll
-    for (int c = 0; c < 8; c++) S[(64 + c) * P + vc] = Rv[c];
+    for (int c = 0; c < 8; c++) S[64 * P + c * P + vc] = Rv[c];
   }
   if (a.needJ) {
 #pragma unroll
@@ -436,8 +462,12 @@ __device__ __forceinline__ void canon_vertex(const DevArgs &a, int block) {
           acc[d] += ed;
         }
       }
-#pragma unroll
-      for (int b = 0; b < 8; b++) S[(c * 8 + b) * P + vc] = acc[b];
+      // J_v[c][0..7] is 64 contiguous bytes at [c][vc][b]
+      double2 *dst = reinterpret_cast<double2 *>(S + ((long long)c * P + vc) * 8);
+      dst[0] = make_double2(acc[0], acc[1]);
+      dst[1] = make_double2(acc[2], acc[3]);
+      dst[2] = make_double2(acc[4], acc[5]);
+      dst[3] = make_double2(acc[6], acc[7]);
     }
   }
 }
@@ -529,34 +559,61 @@ __global__ void __launch_bounds__(128) vertex_kernel(DevArgs a, int canon_blocks
 // with coalesced stores.  Both sum the vertices in the cell's corner order, so
 // a cell gets the same bits on either path.
 __device__ __forceinline__ void struct_cell(const DevArgs &a, int block) {
+  extern __shared__ double rowbuf[];
   const int sidx = block * blockDim.x + threadIdx.x;
-  if (sidx >= a.nS) return;
-  const int i = a.sc_cells[sidx];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (sidx - lane >= a.nS) return;  // whole warp out of range
+  const bool active = sidx < a.nS;
+  const int i = active ? a.sc_cells[sidx] : 0;
   const long long P = a.nCpad, Q = a.nSpad;
-  int vc[8];
-#pragma unroll
-  for (int j = 0; j < 8; j++) vc[j] = a.sc_vc[j * Q + sidx];
   const double *S = a.scratch;
-  if (a.needR) {
-    double s = 0.0;
+  double row[27];
+  if (active) {
+    int vc[8];
 #pragma unroll
-    for (int j = 0; j < 8; j++) s += S[(64 + d_struct_octant(j)) * P + vc[j]];
-    s += a.acc_a[i];
-    s -= a.acc_b[i];
-    a.R[i] = s;
-  }
-  if (a.needJ) {
-    double row[27];
+    for (int j = 0; j < 8; j++) vc[j] = a.sc_vc[j * Q + sidx];
+    if (a.needR) {
+      double s = 0.0;
 #pragma unroll
-    for (int k = 0; k < 27; k++) row[k] = 0.0;
-#pragma unroll
-    for (int j = 0; j < 8; j++) {
-      const double *blk = S + (long long)(d_struct_octant(j) * 8) * P + vc[j];
-#pragma unroll
-      for (int b = 0; b < 8; b++) row[d_struct_slot(j, b)] += blk[b * P];
+      for (int j = 0; j < 8; j++) s += S[64 * P + d_struct_octant(j) * P + vc[j]];
+      s += a.acc_a[i];
+      s -= a.acc_b[i];
+      a.R[i] = s;
     }
-    row[13] += a.jdiag[i];
-    double *out = a.J + a.rowptr[i];
+    if (a.needJ) {
+#pragma unroll
+      for (int k = 0; k < 27; k++) row[k] = 0.0;
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        const double2 *blk = reinterpret_cast<const double2 *>(S + ((long long)d_struct_octant(j) * P + vc[j]) * 8);
+        const double2 v0 = blk[0], v1 = blk[1], v2 = blk[2], v3 = blk[3];
+        row[d_struct_slot(j, 0)] += v0.x;
+        row[d_struct_slot(j, 1)] += v0.y;
+        row[d_struct_slot(j, 2)] += v1.x;
+        row[d_struct_slot(j, 3)] += v1.y;
+        row[d_struct_slot(j, 4)] += v2.x;
+        row[d_struct_slot(j, 5)] += v2.y;
+        row[d_struct_slot(j, 6)] += v3.x;
+        row[d_struct_slot(j, 7)] += v3.y;
+      }
+      row[13] += a.jdiag[i];
+    }
+  }
+  if (!a.needJ) return;
+  // rows of the warp contiguous in the CSR value array: stage and store
+  // coalesced; otherwise every thread stores its own row
+  const int rp = active ? a.rowptr[i] : 0;
+  const int rp0 = __shfl_sync(0xffffffffu, rp, 0);
+  const bool contig = __all_sync(0xffffffffu, active && rp == rp0 + 27 * lane);
+  if (contig) {
+    double *buf = rowbuf + (size_t)warp * 32 * 27;
+#pragma unroll
+    for (int k = 0; k < 27; k++) buf[lane * 27 + k] = row[k];
+    __syncwarp();
+    double *out = a.J + rp0;
+    for (int j = lane; j < 32 * 27; j += 32) out[j] = buf[j];
+  } else if (active) {
+    double *out = a.J + rp;
 #pragma unroll
     for (int k = 0; k < 27; k++) out[k] = row[k];
   }
@@ -668,6 +725,8 @@ int device_setup(_p_TDy *t) {
   UP(a.ss, t->mat.source_sink);
   UP(a.sat_type, t->mat.sat_type);
   UP(a.rp_type, t->mat.relperm_type);
+  UP(a.lam_sat, t->mat.lam_sat);
+  a.vis = t->mat.vis;
   std::vector<int> bnd_cell(m.nb);
   for (int b = 0; b < m.nb; b++) bnd_cell[b] = m.face_cell1[m.bnd_face[b]];
   UP(a.bnd_cell, bnd_cell);
@@ -787,7 +846,7 @@ int device_presolve_host(_p_TDy *t, const double *Uprev) {
 // them for the per-kernel timers.
 static int launch_eval(const DevArgs &a, cudaStream_t st, cudaEvent_t *events) {
   const size_t canon_smem = 36 * 128 * sizeof(double);
-  const size_t cell_smem = 64 * (size_t)a.max_row_nnz * sizeof(double);
+  const size_t cell_smem = 64 * (size_t)(a.max_row_nnz > 27 ? a.max_row_nnz : 27) * sizeof(double);
   const int cb = (int)nblocks(a.nC, 128), gb = (int)nblocks(a.ngen, 128);
   const int sb = (int)nblocks(a.nS, 64), gcb = (int)nblocks(a.ngc, 64);
   if (events) CUDA_TRY(cudaEventRecord(events[0], st));
@@ -818,7 +877,7 @@ int device_eval(_p_TDy *t, int form, double time, const double *dU, const double
   a.U = dU;
   a.Ut = dUt;
   a.dt = t->dtime;
-  a.shift = shift;
+  a.shift = form == FORM_SNES ? 1.0 / t->dtime : shift;
   a.needR = dR != nullptr;
   a.needJ = dJ != nullptr;
   a.R = dR;
@@ -975,7 +1034,7 @@ int device_eval_noalloc(_p_TDy *t, const double *dU, double *dR, double *dJ, voi
   a.U = dU;
   a.Ut = nullptr;
   a.dt = t->dtime;
-  a.shift = 0.0;
+  a.shift = 1.0 / t->dtime;
   a.needR = dR != nullptr;
   a.needJ = dJ != nullptr;
   a.R = dR;

@@ -555,9 +555,9 @@ int mpfao_setup(const Options &opt, const Mesh &m, const Materials &mat, const B
         if (cols[k] == c) a = k;
       if (a < 0) return set_error(TDY_ERR_LIB, "cell %d missing at its vertex %d", c, v);
       if (canon_idx[v] >= 0) {
-        s.cv_jbase.push_back((long long)(a * 8) * P + canon_idx[v]);
-        s.cv_rbase.push_back((long long)(64 + a) * P + canon_idx[v]);
-        s.cv_stride.push_back((int)P);
+        s.cv_jbase.push_back(((long long)a * P + canon_idx[v]) * 8);
+        s.cv_rbase.push_back(64 * P + (long long)a * P + canon_idx[v]);
+        s.cv_stride.push_back(1);
       } else {
         s.cv_jbase.push_back(s.v_jv_off[v] + (long long)a * nint);
         s.cv_rbase.push_back(s.v_jv_off[v] + (long long)nint * nint + a);
