@@ -109,11 +109,12 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def build_workload(host_only=False, grid=None):
+def build_workload(host_only=False, grid=None, jacobian_arithmetic="FP64"):
     import tdycore_gb300 as T
     from tdycore_gb300.workloads import spe10_like
 
     T.options_clear()
+    T.options_insert(f"-tdy_jacobian_arithmetic {jacobian_arithmetic}")
     t0 = time.perf_counter()
     if grid:
         nx, ny, nz = grid
@@ -224,7 +225,7 @@ def run_gpu(args, rank, world, local_rank):
         import torch.distributed as dist
 
         dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
-    t, U, Uprev, info = build_workload(grid=args.grid)
+    t, U, Uprev, info = build_workload(grid=args.grid, jacobian_arithmetic=args.jacobian_arithmetic)
     view = t.setup_view()
     nc, nnz = t.ncells, t.nnz
     t.set_dtime(DT)
@@ -324,7 +325,8 @@ def run_gpu(args, rank, world, local_rank):
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": info["workload"], "ncells": nc, "nnz_jacobian": nnz, "form": "SNES F+J",
                        "seed": info["seed"], "l2": "inputs larger than L2 (no flush)",
-                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                       "jacobian_arithmetic": args.jacobian_arithmetic},
             "roofline": {"bound": "hbm", "kernel": "vertex_kernel", "achieved": achieved, "peak": hbm_peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm_peak,
                          "traffic": traffic, "algorithmic_bytes_per_launch": vb,
@@ -358,6 +360,8 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--grid", type=int, nargs=3, default=None, metavar=("NX", "NY", "NZ"),
                     help="smaller grid with the same extents per cell (profiling captures)")
+    ap.add_argument("--jacobian-arithmetic", default="FP64", choices=["DOUBLE_FLOAT", "FP64"],
+                    help="arithmetic of the Jacobian products at interior hexahedral vertices")
     ap.add_argument("--profile", action="store_true",
                     help="time the device loop only (no timers, e2e, CPU or clock-fill loops), for ncu")
     args = ap.parse_args()

@@ -256,6 +256,7 @@ TDyErrorCode TDySetFromOptions(TDy tdy) {
   static const char *const visc[] = {"CONSTANT", "BATZLE_AND_WANG"};
   static const char *const gm[] = {"MPFAO_GMATRIX_DEFAULT", "MPFAO_GMATRIX_TPF"};
   static const char *const bct[] = {"DIRICHLET_BC", "NEUMANN_BC", "SEEPAGE_BC"};
+  static const char *const jarith[] = {"DOUBLE_FLOAT", "FP64"};
   int ierr;
   // option names as spelled in src/tdycore.c:525-540 and tdympfao.c:584-596
   if ((ierr = opt_real("-tdy_porosity", &o.porosity))) return ierr;
@@ -269,6 +270,8 @@ TDyErrorCode TDySetFromOptions(TDy tdy) {
   if ((ierr = opt_enum("-tdy_water_viscosity", visc, 2, &o.mu_type))) return ierr;
   if ((ierr = opt_enum("-tdy_mpfao_gmatrix_method", gm, 2, &o.gmatrix_method))) return ierr;
   if ((ierr = opt_enum("-tdy_mpfao_boundary_condition_type", bct, 3, &o.bc_type))) return ierr;
+  // extension: arithmetic of the Jacobian products (FP64 residual either way)
+  if ((ierr = opt_enum("-tdy_jacobian_arithmetic", jarith, 2, &o.jacobian_arithmetic))) return ierr;
   double pbc;
   if (opt_find("-tdy_pressure_bc_value", nullptr)) {
     if ((ierr = opt_real("-tdy_pressure_bc_value", &pbc))) return ierr;

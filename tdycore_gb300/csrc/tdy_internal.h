@@ -22,6 +22,9 @@ int set_error(int code, const char *fmt, ...);
 // ---------------------------------------------------------------------------
 // Options (reference: src/tdycore.c:260-296 SetDefaultOptions and
 // src/fv/mpfao/tdympfao.c:428-444 TDyCreate_MPFAO).
+// -tdy_jacobian_arithmetic values (extension; the reference has FP64 only)
+enum { JACOBIAN_DOUBLE_FLOAT = 0, JACOBIAN_FP64 = 1 };
+
 struct Options {
   double gravity = 9.8068;
   double porosity = 0.25;
@@ -42,6 +45,8 @@ struct Options {
   double Tref = 25.0;
   bool has_pressure_bc_value = false;
   double pressure_bc_value = 0.0;
+  // arithmetic of the Jacobian products w*T at interior hexahedral vertices
+  int jacobian_arithmetic = JACOBIAN_FP64;
 };
 
 // How a per-cell property is specified by the user.

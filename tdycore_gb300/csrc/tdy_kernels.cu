@@ -34,6 +34,8 @@
 // (tdympfao_ts.c:116-118, 404-417) regrouped to need fewer FP64 operations.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -41,6 +43,7 @@
 #include <vector>
 
 #include "tdy_device.h"
+#include "tdy_ff.h"
 
 namespace tdy {
 
@@ -75,6 +78,7 @@ struct DevArgs {
   // canonical interior-hex vertices (SoA, stride nCpad)
   int nC, nCpad;
   const double *Tc;
+  int jac_ff;  // Jacobian products of canonical vertices in double-float
   const int *cellc, *facec;
   // generic vertices
   int ngen;
@@ -379,7 +383,7 @@ __host__ __device__ constexpr int canon_row(int c, int k) {
 }
 __host__ __device__ constexpr bool canon_is_up(int c, int k) { return ((c >> k) & 1) == 0; }
 
-template <bool CONST_RHO>
+template <bool CONST_RHO, bool FFJ>
 __device__ __forceinline__ void canon_vertex(const DevArgs &a, int block) {
   extern __shared__ double sh[];  // [36][blockDim]: w, E_up, E_dn per row
   const int tid = threadIdx.x, bs = blockDim.x;
@@ -417,15 +421,18 @@ __device__ __forceinline__ void canon_vertex(const DevArgs &a, int block) {
     Rv[u] += flux;
     Rv[d] -= flux;
     if (a.needJ) {
-      const double dlu = fdn ? dlam[u] : 0.0, dld = fdn ? 0.0 : dlam[d];
+      // derivative of the flux with respect to the up and down cell pressures
+      // beyond w*T: d(rho_avg)/dP and d(kr/mu)/dP of the upwind cell
       double eu, ed;
       if (CONST_RHO) {
-        eu = den * dlu * q;
-        ed = den * dld * q;
+        const double e = __dmul_rn(__dmul_rn(den, q), fdn ? dlam[u] : dlam[d]);
+        eu = fdn ? e : 0.0;
+        ed = fdn ? 0.0 : e;
       } else {
-        const double g2 = q + den * G;
-        eu = hdr[u] * lm * g2 + den * dlu * q;
-        ed = hdr[d] * lm * g2 + den * dld * q;
+        const double dlu = fdn ? dlam[u] : 0.0, dld = fdn ? 0.0 : dlam[d];
+        const double g2 = __fma_rn(den, G, q);
+        eu = __fma_rn(__dmul_rn(hdr[u], lm), g2, __dmul_rn(__dmul_rn(den, dlu), q));
+        ed = __fma_rn(__dmul_rn(hdr[d], lm), g2, __dmul_rn(__dmul_rn(den, dld), q));
       }
       sh[r * bs + tid] = w;
       sh[(12 + r) * bs + tid] = eu;
@@ -437,12 +444,72 @@ __device__ __forceinline__ void canon_vertex(const DevArgs &a, int block) {
 #pragma unroll
     for (int c = 0; c < 8; c++) S[64 * P + c * P + vc] = Rv[c];
   }
-  if (a.needJ) {
+  if (!a.needJ) return;
+  // J_v[c][b] = sum over the three rows k of octant c of
+  //   -+ w_r T_rb  (minus when c is the row's up cell)  -+ E terms
+  if (FFJ) {
+    // Octants in a runtime loop (keeps the code small enough for the
+    // instruction cache); entries are indexed relative to the octant,
+    // j = b ^ c, so the row of axis k touches entries 0 (c itself) and 1 << k
+    // at compile-time register indices.
+#pragma unroll 1
+    for (int c = 0; c < 8; c++) {
+      // Each entry is accumulated at its own power-of-two scale, chosen from
+      // the exponent fields of its terms so that its largest term is O(1):
+      // entries of rows upwinded from nearly dry cells (kr ~ 1e-30 and
+      // below) keep full relative accuracy next to O(1) entries.
+      double wk[3], es[3], en[3], Tk[3][8];
+      int bw[3], mb[8];
+#pragma unroll
+      for (int j = 0; j < 8; j++) mb[j] = 0;
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        const int r = canon_row(c, k);
+        const bool up = canon_is_up(c, k);
+        wk[k] = sh[r * bs + tid];
+        bw[k] = d_bexp(wk[k]);
+        const double eu = sh[(12 + r) * bs + tid], ed = sh[(24 + r) * bs + tid];
+        es[k] = up ? eu : ed;  // E term of c itself
+        en[k] = up ? ed : eu;  // E term of the neighbour c ^ (1 << k)
+        const double *T = a.Tc + (long long)(r * 8) * P + vc;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          Tk[k][j] = T[(j ^ c) * P];
+          const int bt = d_bexp(Tk[k][j]);
+          mb[j] = max(mb[j], (bw[k] && bt) ? bw[k] + bt - 1023 : 0);
+        }
+        mb[0] = max(mb[0], d_bexp(es[k]));
+        mb[1 << k] = max(mb[1 << k], d_bexp(en[k]));
+      }
+      ff acc[8];
+#pragma unroll
+      for (int j = 0; j < 8; j++) acc[j] = ff{0.0f, 0.0f};
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        const bool up = canon_is_up(c, k);
+        // w normalised to [1, 2); T carries the rest of the entry's scale
+        ff wf = ff_split(wk[k], 1023 - bw[k]);
+        ff ef = ff_split(es[k], 1023 - mb[0]), nf = ff_split(en[k], 1023 - mb[1 << k]);
+        if (up) {
+          wf = ff_neg(wf);
+          ef = ff_neg(ef);
+          nf = ff_neg(nf);
+        }
+#pragma unroll
+        for (int j = 0; j < 8; j++) ff_acc(acc[j], ff_mul(wf, ff_split(Tk[k][j], bw[k] - mb[j])));
+        ff_acc(acc[0], ef);
+        ff_acc(acc[1 << k], nf);
+      }
+      double *dst = S + ((long long)c * P + vc) * 8;
+#pragma unroll
+      for (int j = 0; j < 8; j++) dst[j ^ c] = ff_to_d(acc[j], mb[j] - 1023);
+    }
+  } else {
 #pragma unroll
     for (int c = 0; c < 8; c++) {
-      double acc[8];
+      double out[8];
 #pragma unroll
-      for (int b = 0; b < 8; b++) acc[b] = 0.0;
+      for (int b = 0; b < 8; b++) out[b] = 0.0;
 #pragma unroll
       for (int k = 0; k < 3; k++) {
         const int r = canon_row(c, k);
@@ -451,23 +518,18 @@ __device__ __forceinline__ void canon_vertex(const DevArgs &a, int block) {
         const double sw = up ? -wr : wr;
         const double *T = a.Tc + (long long)(r * 8) * P + vc;
 #pragma unroll
-        for (int b = 0; b < 8; b++) acc[b] = fma(sw, T[b * P], acc[b]);
+        for (int b = 0; b < 8; b++) out[b] = __fma_rn(sw, T[b * P], out[b]);
         const double eu = sh[(12 + r) * bs + tid], ed = sh[(24 + r) * bs + tid];
         const int u = canon_up(r), d = canon_dn(r);
-        if (up) {
-          acc[u] -= eu;
-          acc[d] -= ed;
-        } else {
-          acc[u] += eu;
-          acc[d] += ed;
-        }
+        out[u] = __dadd_rn(out[u], up ? -eu : eu);
+        out[d] = __dadd_rn(out[d], up ? -ed : ed);
       }
       // J_v[c][0..7] is 64 contiguous bytes at [c][vc][b]
       double2 *dst = reinterpret_cast<double2 *>(S + ((long long)c * P + vc) * 8);
-      dst[0] = make_double2(acc[0], acc[1]);
-      dst[1] = make_double2(acc[2], acc[3]);
-      dst[2] = make_double2(acc[4], acc[5]);
-      dst[3] = make_double2(acc[6], acc[7]);
+      dst[0] = make_double2(out[0], out[1]);
+      dst[1] = make_double2(out[2], out[3]);
+      dst[2] = make_double2(out[4], out[5]);
+      dst[3] = make_double2(out[6], out[7]);
     }
   }
 }
@@ -542,10 +604,10 @@ __device__ __forceinline__ void generic_vertex(const DevArgs &a, int block) {
 }
 
 // Canonical vertices take the first blocks of the launch, the others the rest.
-template <bool CONST_RHO>
+template <bool CONST_RHO, bool FFJ>
 __global__ void __launch_bounds__(128) vertex_kernel(DevArgs a, int canon_blocks) {
   if ((int)blockIdx.x < canon_blocks)
-    canon_vertex<CONST_RHO>(a, blockIdx.x);
+    canon_vertex<CONST_RHO, FFJ>(a, blockIdx.x);
   else
     generic_vertex(a, blockIdx.x - canon_blocks);
 }
@@ -747,6 +809,7 @@ int device_setup(_p_TDy *t) {
   a.nC = s.nC;
   a.nCpad = s.nCpad;
   UP(a.Tc, s.Tc);
+  a.jac_ff = t->opt.jacobian_arithmetic == JACOBIAN_DOUBLE_FLOAT;
   UP(a.cellc, s.cellc);
   UP(a.facec, s.facec);
   a.ngen = (int)s.gen_vertex.size();
@@ -853,10 +916,15 @@ static int launch_eval(const DevArgs &a, cudaStream_t st, cudaEvent_t *events) {
   state_kernel<<<nblocks(a.nc + a.nb, 256), 256, 0, st>>>(a);
   if (events) CUDA_TRY(cudaEventRecord(events[1], st));
   if (cb + gb > 0) {
-    if (a.rho_type == WATER_DENSITY_EXPONENTIAL)
-      vertex_kernel<false><<<cb + gb, 128, canon_smem, st>>>(a, cb);
+    const bool cr = a.rho_type != WATER_DENSITY_EXPONENTIAL;
+    if (cr && a.jac_ff)
+      vertex_kernel<true, true><<<cb + gb, 128, canon_smem, st>>>(a, cb);
+    else if (cr)
+      vertex_kernel<true, false><<<cb + gb, 128, canon_smem, st>>>(a, cb);
+    else if (a.jac_ff)
+      vertex_kernel<false, true><<<cb + gb, 128, canon_smem, st>>>(a, cb);
     else
-      vertex_kernel<true><<<cb + gb, 128, canon_smem, st>>>(a, cb);
+      vertex_kernel<false, false><<<cb + gb, 128, canon_smem, st>>>(a, cb);
   }
   if (events) CUDA_TRY(cudaEventRecord(events[2], st));
   if (sb + gcb > 0) cell_kernel<<<sb + gcb, 64, cell_smem, st>>>(a, sb);

@@ -13,6 +13,16 @@ from tdycore_gb300 import workloads as W
 
 PREF = 101325.0
 
+# options inserted after every case's options_clear(); the parity tests set
+# it to select the Jacobian arithmetic
+EXTRA_OPTIONS = ""
+
+
+def _clear():
+    T.options_clear()
+    if EXTRA_OPTIONS:
+        T.options_insert(EXTRA_OPTIONS)
+
 
 def _states(n, rng, center, spread):
     U = center + rng.normal(0.0, spread, n)
@@ -22,14 +32,14 @@ def _states(n, rng, center, spread):
 
 
 def case_column():
-    T.options_clear()
+    _clear()
     t = W.box_column(1, 1, 15)
     rng = np.random.default_rng(1)
     return (t, *_states(15, rng, 102325.0, 3e3))
 
 
 def case_tpf_dirichlet():
-    T.options_clear()
+    _clear()
     t = W.box_column(5, 5, 5, gmatrix=T.MPFAO_GMATRIX_TPF, bc_type=T.DIRICHLET_BC,
                      pfunc=lambda x, y, z: 110000.0 if z > 0.99 else 100000.0)
     rng = np.random.default_rng(2)
@@ -37,28 +47,28 @@ def case_tpf_dirichlet():
 
 
 def case_seepage():
-    T.options_clear()
+    _clear()
     t = W.box_column(4, 3, 5, bc_type=T.SEEPAGE_BC, pfunc=lambda x, y, z: 99000.0 if x < 0.5 else 104000.0)
     rng = np.random.default_rng(3)
     return (t, *_states(60, rng, 101325.0, 6e3))
 
 
 def case_neumann():
-    T.options_clear()
+    _clear()
     t = W.box_column(3, 3, 3, density=T.WATER_DENSITY_CONSTANT, bc_type=T.NEUMANN_BC)
     rng = np.random.default_rng(4)
     return (t, *_states(27, rng, 95000.0, 5e3))
 
 
 def case_single_cell():
-    T.options_clear()
+    _clear()
     t = W.box_column(1, 1, 1, pfunc=lambda x, y, z: 100500.0)
     rng = np.random.default_rng(5)
     return (t, *_states(1, rng, 101000.0, 1e3))
 
 
 def case_spe10_small():
-    T.options_clear()
+    _clear()
     t, U, _ = W.spe10_like(12, 10, 8, lx=73.152, ly=30.48, lz=4.8768, seed_offset=7)
     rng = np.random.default_rng(6)
     n = U.size
@@ -66,7 +76,7 @@ def case_spe10_small():
 
 
 def case_wedge():
-    T.options_clear()
+    _clear()
     t, U, _ = W.wedge_extruded(npts=40, nlayers=3, seed_offset=1)
     rng = np.random.default_rng(7)
     n = U.size
@@ -75,7 +85,7 @@ def case_wedge():
 
 def case_mixed_curves():
     """Gardner saturation and Irmay kr on some cells, Batzle-Wang EOS."""
-    T.options_clear()
+    _clear()
     t = W.box_column(4, 4, 4, density=T.WATER_DENSITY_BATZLE_AND_WANG)
     t.set_water_viscosity_type(T.WATER_VISCOSITY_BATZLE_AND_WANG)
     cells = np.arange(0, 64, 3)
@@ -88,7 +98,7 @@ def case_mixed_curves():
 
 
 def case_hydrostatic_box():
-    T.options_clear()
+    _clear()
     t, U0, _ = W.hydrostatic_box(10)
     rng = np.random.default_rng(9)
     n = U0.size

@@ -12,6 +12,7 @@ import numpy as np
 import pytest
 
 from oracle import Oracle
+from tests import parity_cases
 from tests.parity_cases import CASES
 
 pytestmark = pytest.mark.gpu
@@ -21,8 +22,17 @@ J_TOL = 1e-10
 DT = 1800.0
 
 
-def _setup(name):
-    t, U, Uprev, Ut = CASES[name]()
+# Jacobian products at interior hexahedral vertices: FP64 (default) or
+# double-float; both must meet the same bars
+ARITH = ["FP64", "DOUBLE_FLOAT"]
+
+
+def _setup(name, arith="FP64"):
+    parity_cases.EXTRA_OPTIONS = f"-tdy_jacobian_arithmetic {arith}"
+    try:
+        t, U, Uprev, Ut = CASES[name]()
+    finally:
+        parity_cases.EXTRA_OPTIONS = ""
     t.setup()
     o = Oracle(t.setup_view())
     return t, o, U, Uprev, Ut
@@ -36,9 +46,10 @@ def assert_close(got, ref, mag, tol, what):
                            f" err {err[bad].max():.3e} mag {mag[bad].max():.3e}")
 
 
+@pytest.mark.parametrize("arith", ARITH)
 @pytest.mark.parametrize("name", list(CASES))
-def test_snes_parity(name):
-    t, o, U, Uprev, _ = _setup(name)
+def test_snes_parity(name, arith):
+    t, o, U, Uprev, _ = _setup(name, arith)
     rp, ci = o.pattern()
     assert np.array_equal(rp, t.rowptr) and np.array_equal(ci, t.colidx), "CSR pattern differs"
     t.set_dtime(DT)
@@ -54,9 +65,10 @@ def test_snes_parity(name):
     assert np.array_equal(t.snes_jacobian(U), J)
 
 
+@pytest.mark.parametrize("arith", ARITH)
 @pytest.mark.parametrize("name", list(CASES))
-def test_ts_parity(name):
-    t, o, U, _, Ut = _setup(name)
+def test_ts_parity(name, arith):
+    t, o, U, _, Ut = _setup(name, arith)
     shift = 1.0 / 100.0
     R, J = t.ifunction_ijacobian(0.0, U, Ut, shift)
     Rr, Rm = o.ts_ifunction(U, Ut, with_mag=True)
@@ -99,3 +111,21 @@ def test_jacobian_is_derivative_of_residual():
     Jd = np.bincount(rows, weights=J * d[t.colidx], minlength=n)
     scale = np.abs(Jd).max()
     assert np.abs(fd - Jd).max() <= 1e-5 * scale
+
+
+@pytest.mark.parametrize("name", ["spe10_small", "hydrostatic_box", "mixed_curves"])
+def test_double_float_jacobian_tracks_fp64(name):
+    """The double-float Jacobian products stay within 1e-12 of the error scale
+    of the FP64 ones (two orders inside the parity bar); residuals are FP64 in
+    both and identical."""
+    runs = {}
+    for arith in ARITH:
+        t, o, U, Uprev, _ = _setup(name, arith)
+        t.set_dtime(DT)
+        t.presolve(Uprev)
+        o.snes_presolve(Uprev, DT)
+        runs[arith] = t.snes_function_jacobian(U)
+    _, Jm = o.snes_jacobian(U, with_mag=True)
+    (Rf, Jf), (Rd, Jd) = runs["DOUBLE_FLOAT"], runs["FP64"]
+    assert np.array_equal(Rf, Rd)
+    assert_close(Jf, Jd, Jm, 1e-12, f"{name} double-float vs FP64 Jacobian")
