@@ -109,7 +109,7 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def build_workload(host_only=False, grid=None, jacobian_arithmetic="FP64"):
+def build_workload(host_only=False, grid=None, jacobian_arithmetic="DOUBLE_FLOAT"):
     import tdycore_gb300 as T
     from tdycore_gb300.workloads import spe10_like
 
@@ -360,7 +360,7 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--grid", type=int, nargs=3, default=None, metavar=("NX", "NY", "NZ"),
                     help="smaller grid with the same extents per cell (profiling captures)")
-    ap.add_argument("--jacobian-arithmetic", default="FP64", choices=["DOUBLE_FLOAT", "FP64"],
+    ap.add_argument("--jacobian-arithmetic", default="DOUBLE_FLOAT", choices=["DOUBLE_FLOAT", "FP64"],
                     help="arithmetic of the Jacobian products at interior hexahedral vertices")
     ap.add_argument("--profile", action="store_true",
                     help="time the device loop only (no timers, e2e, CPU or clock-fill loops), for ncu")

@@ -55,6 +55,23 @@ __device__ __forceinline__ ff ff_split(double x, int s) {
   return r;
 }
 
+// x * 2^s as hi + lo for the Jacobian products, given bx = d_bexp(x) and
+// the scale s, with fewer operations than ff_split: hi is x truncated to 24
+// bits, lo the next 23 significand bits (unnormalised), so |error| < 2^-46
+// |x|.  Callers choose s so that |x| 2^s < 4; parts that fall below the float
+// normal range come out as subnormal or zero floats of magnitude < 2^-126.
+__device__ __forceinline__ ff ff_split_scaled(double x, int bx, int s) {
+  const unsigned hw = (unsigned)__double2hiint(x), lw = (unsigned)__double2loint(x);
+  const unsigned sign = hw & 0x80000000u;
+  const int fe = bx ? max(bx + s - 896, 0) : 0;  // float biased exponent of hi
+  ff r;
+  r.h = __uint_as_float(sign | ((unsigned)fe << 23) | (__funnelshift_l(lw, hw, 3) & 0x7fffffu));
+  // (the 23 bits below hi) * 2^-23 exactly, in [0, 1)
+  const float frac = __fadd_rn(__uint_as_float(0x3f800000u | ((lw >> 6) & 0x7fffffu)), -1.0f);
+  r.l = __fmul_rn(frac, __uint_as_float(sign | ((unsigned)max(fe - 23, 0) << 23)));
+  return r;
+}
+
 // exact float -> double times 2^s (zero, subnormal and underflowing inputs
 // give signed zero)
 __device__ __forceinline__ double ff_f2d(float f, int s) {

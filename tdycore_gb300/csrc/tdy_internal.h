@@ -46,7 +46,7 @@ struct Options {
   bool has_pressure_bc_value = false;
   double pressure_bc_value = 0.0;
   // arithmetic of the Jacobian products w*T at interior hexahedral vertices
-  int jacobian_arithmetic = JACOBIAN_FP64;
+  int jacobian_arithmetic = JACOBIAN_DOUBLE_FLOAT;
 };
 
 // How a per-cell property is specified by the user.

@@ -239,8 +239,15 @@ __device__ __forceinline__ void viscosity(int type, double *vis, double *dvis) {
 
 // ---------------------------------------------------------------------------
 // 1. cell and boundary-face state
-__global__ void __launch_bounds__(256) state_kernel(DevArgs a) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
+// Warps take 32-entity chunks in the order chunk = (warp * chunk_mul) mod
+// nchunks (chunk_mul coprime to nchunks): loads stay coalesced within a warp
+// while the unsaturated cells, which cost ~50x more and cluster in space
+// (and therefore in cell numbering), spread over every SM instead of forming
+// a tail of a few slow blocks.
+__global__ void __launch_bounds__(256) state_kernel(DevArgs a, int nchunks, int chunk_mul) {
+  const int gw = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  if (gw >= nchunks) return;
+  const int i = (int)(((long long)gw * chunk_mul) % nchunks) * 32 + (threadIdx.x & 31);
   if (i < a.nc) {
     const double U = a.U[i];
     const double Pc = a.Pref - U;
@@ -459,7 +466,7 @@ __device__ __forceinline__ void canon_vertex(const DevArgs &a, int block) {
       // entries of rows upwinded from nearly dry cells (kr ~ 1e-30 and
       // below) keep full relative accuracy next to O(1) entries.
       double wk[3], es[3], en[3], Tk[3][8];
-      int bw[3], mb[8];
+      int bw[3], bt[3][8], mb[8];
 #pragma unroll
       for (int j = 0; j < 8; j++) mb[j] = 0;
 #pragma unroll
@@ -475,8 +482,9 @@ __device__ __forceinline__ void canon_vertex(const DevArgs &a, int block) {
 #pragma unroll
         for (int j = 0; j < 8; j++) {
           Tk[k][j] = T[(j ^ c) * P];
-          const int bt = d_bexp(Tk[k][j]);
-          mb[j] = max(mb[j], (bw[k] && bt) ? bw[k] + bt - 1023 : 0);
+          bt[k][j] = d_bexp(Tk[k][j]);
+          // biased exponent of |w T| (a zero factor gives a negligible value)
+          mb[j] = max(mb[j], bw[k] + bt[k][j] - 1023);
         }
         mb[0] = max(mb[0], d_bexp(es[k]));
         mb[1 << k] = max(mb[1 << k], d_bexp(en[k]));
@@ -488,15 +496,16 @@ __device__ __forceinline__ void canon_vertex(const DevArgs &a, int block) {
       for (int k = 0; k < 3; k++) {
         const bool up = canon_is_up(c, k);
         // w normalised to [1, 2); T carries the rest of the entry's scale
-        ff wf = ff_split(wk[k], 1023 - bw[k]);
-        ff ef = ff_split(es[k], 1023 - mb[0]), nf = ff_split(en[k], 1023 - mb[1 << k]);
+        ff wf = ff_split_scaled(wk[k], bw[k], 1023 - bw[k]);
+        ff ef = ff_split_scaled(es[k], d_bexp(es[k]), 1023 - mb[0]);
+        ff nf = ff_split_scaled(en[k], d_bexp(en[k]), 1023 - mb[1 << k]);
         if (up) {
           wf = ff_neg(wf);
           ef = ff_neg(ef);
           nf = ff_neg(nf);
         }
 #pragma unroll
-        for (int j = 0; j < 8; j++) ff_acc(acc[j], ff_mul(wf, ff_split(Tk[k][j], bw[k] - mb[j])));
+        for (int j = 0; j < 8; j++) ff_acc(acc[j], ff_mul(wf, ff_split_scaled(Tk[k][j], bt[k][j], bw[k] - mb[j])));
         ff_acc(acc[0], ef);
         ff_acc(acc[1 << k], nf);
       }
@@ -603,13 +612,14 @@ __device__ __forceinline__ void generic_vertex(const DevArgs &a, int block) {
   }
 }
 
-// Canonical vertices take the first blocks of the launch, the others the rest.
+// The other (heavier, per-vertex-block) vertices take the first blocks of the
+// launch so they overlap the canonical ones instead of trailing them.
 template <bool CONST_RHO, bool FFJ>
-__global__ void __launch_bounds__(128) vertex_kernel(DevArgs a, int canon_blocks) {
-  if ((int)blockIdx.x < canon_blocks)
-    canon_vertex<CONST_RHO, FFJ>(a, blockIdx.x);
+__global__ void __launch_bounds__(128) vertex_kernel(DevArgs a, int gen_blocks) {
+  if ((int)blockIdx.x >= gen_blocks)
+    canon_vertex<CONST_RHO, FFJ>(a, blockIdx.x - gen_blocks);
   else
-    generic_vertex(a, blockIdx.x - canon_blocks);
+    generic_vertex(a, blockIdx.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -886,6 +896,23 @@ int device_upload_source_sink(_p_TDy *t) {
 
 static inline unsigned nblocks(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
+// A multiplier coprime to n near 0.618 n (golden-ratio stride), so that
+// chunk -> chunk * m mod n is a permutation that scatters neighbouring chunks.
+static int chunk_multiplier(int n) {
+  if (n <= 2) return 1;
+  long long m = (long long)(0.6180339887 * n) | 1;
+  auto gcd = [](long long x, long long y) {
+    while (y) {
+      long long t = x % y;
+      x = y;
+      y = t;
+    }
+    return x;
+  };
+  while (gcd(m, n) != 1) m += 2;
+  return (int)(m % n);
+}
+
 int device_presolve(_p_TDy *t, const double *dUprev, void *stream) {
   DeviceState *d = t->dev;
   cudaStream_t st = stream ? (cudaStream_t)stream : d->stream;
@@ -913,18 +940,21 @@ static int launch_eval(const DevArgs &a, cudaStream_t st, cudaEvent_t *events) {
   const int cb = (int)nblocks(a.nC, 128), gb = (int)nblocks(a.ngen, 128);
   const int sb = (int)nblocks(a.nS, 64), gcb = (int)nblocks(a.ngc, 64);
   if (events) CUDA_TRY(cudaEventRecord(events[0], st));
-  state_kernel<<<nblocks(a.nc + a.nb, 256), 256, 0, st>>>(a);
+  {
+    const int nchunks = (int)nblocks(a.nc + a.nb, 32);
+    state_kernel<<<nblocks((long long)nchunks * 32, 256), 256, 0, st>>>(a, nchunks, chunk_multiplier(nchunks));
+  }
   if (events) CUDA_TRY(cudaEventRecord(events[1], st));
   if (cb + gb > 0) {
     const bool cr = a.rho_type != WATER_DENSITY_EXPONENTIAL;
     if (cr && a.jac_ff)
-      vertex_kernel<true, true><<<cb + gb, 128, canon_smem, st>>>(a, cb);
+      vertex_kernel<true, true><<<cb + gb, 128, canon_smem, st>>>(a, gb);
     else if (cr)
-      vertex_kernel<true, false><<<cb + gb, 128, canon_smem, st>>>(a, cb);
+      vertex_kernel<true, false><<<cb + gb, 128, canon_smem, st>>>(a, gb);
     else if (a.jac_ff)
-      vertex_kernel<false, true><<<cb + gb, 128, canon_smem, st>>>(a, cb);
+      vertex_kernel<false, true><<<cb + gb, 128, canon_smem, st>>>(a, gb);
     else
-      vertex_kernel<false, false><<<cb + gb, 128, canon_smem, st>>>(a, cb);
+      vertex_kernel<false, false><<<cb + gb, 128, canon_smem, st>>>(a, gb);
   }
   if (events) CUDA_TRY(cudaEventRecord(events[2], st));
   if (sb + gcb > 0) cell_kernel<<<sb + gcb, 64, cell_smem, st>>>(a, sb);
