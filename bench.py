@@ -162,15 +162,32 @@ def fp64_flops_per_eval(view):
     return tp + jac + rows + gather
 
 
-def cpu_baseline(view, U, Uprev, budget_s=12.0, threads=None):
-    """Oracle F+J (reference loop order, colour-parallel) on the host cores."""
+def make_oracle(view, Uprev):
     from oracle import Oracle
 
-    cores = threads or len(os.sched_getaffinity(0))
     t0 = time.perf_counter()
     o = Oracle(view)
     o.snes_presolve(Uprev, DT)
-    log(f"oracle ready in {time.perf_counter() - t0:.1f} s; timing on {cores} threads")
+    log(f"oracle ready in {time.perf_counter() - t0:.1f} s")
+    return o
+
+
+def parity_full_size(o, U, R, J):
+    """Largest error of the GPU R and J against the oracle at the bench
+    workload, in units of the oracle's per-entry error scale (the parity tests
+    require <= 1e-12 for R and <= 1e-10 for J)."""
+    Rr, Rm = o.snes_function(U, with_mag=True)
+    Jr, Jm = o.snes_jacobian(U, with_mag=True)
+    tiny = np.finfo(float).tiny
+    return (float(np.max(np.abs(R - Rr) / np.maximum(Rm, tiny))),
+            float(np.max(np.abs(J - Jr) / np.maximum(Jm, tiny))))
+
+
+def cpu_baseline(o, U, budget_s=12.0, threads=None):
+    ncells = U.size
+    """Oracle F+J (reference loop order, colour-parallel) on the host cores."""
+    cores = threads or len(os.sched_getaffinity(0))
+    log(f"CPU baseline on {cores} threads")
     o.snes_function_jacobian_parallel(U, cores)  # warm-up
     n, t0 = 0, time.perf_counter()
     while True:
@@ -179,7 +196,7 @@ def cpu_baseline(view, U, Uprev, budget_s=12.0, threads=None):
         el = time.perf_counter() - t0
         if el >= budget_s or n >= 50:
             break
-    return view["ncells"] * n / el, cores, n, el
+    return ncells * n / el, cores, n, el
 
 
 def run_reference(args, rank):
@@ -300,6 +317,36 @@ def run_gpu(args, rank, world, local_rank):
         e2e_s = float(te.item())
     e2e_value = world * nc * e2e_steps / e2e_s
 
+    # the same device loop with FP64 Jacobian products, for comparison
+    R_main, J_main = dR.cpu().numpy(), dJ.cpu().numpy()
+    alt = None
+    if args.jacobian_arithmetic != "FP64":
+        t.destroy()
+        del t
+        t2, _, _, _ = build_workload(grid=args.grid, jacobian_arithmetic="FP64")
+        t2.set_dtime(DT)
+        t2.presolve_device(dUp, stream=sp)
+        for _ in range(max(3, args.warmup)):
+            t2.snes_function_jacobian_device(dU, dR, dJ, stream=sp)
+        torch.cuda.synchronize(dev)
+        if dist:
+            dist.barrier()
+        e0.record(stream)
+        for _ in range(args.steps):
+            t2.snes_function_jacobian_device(dU, dR, dJ, stream=sp)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms2 = e0.elapsed_time(e1)
+        if dist:
+            tms = torch.tensor([ms2], device=dev)
+            dist.all_reduce(tms, op=dist.ReduceOp.MAX)
+            ms2 = float(tms.item())
+        alt = {"jacobian_arithmetic": "FP64", "value": world * nc * args.steps / (ms2 * 1e-3),
+               "ms_per_step": ms2 / args.steps, "R": dR.cpu().numpy(), "J": dJ.cpu().numpy()}
+        launches = t2.launches_per_evaluation()
+    else:
+        launches = t.launches_per_evaluation()
+
     if rank == 0:
         hbm_peak, peak_kind = peaks()
         try:
@@ -318,7 +365,16 @@ def run_gpu(args, rank, world, local_rank):
                 traffic = json.loads(tf.read_text()).get("bytes_per_launch_full_workload")
             except Exception:
                 traffic = None
-        cpu_v, cores, n_cpu, cpu_s = cpu_baseline(view, U, Uprev, budget_s=args.cpu_budget)
+        o = make_oracle(view, Uprev)
+        parity = {}
+        parity["R_err_over_scale"], parity[f"J_err_over_scale_{args.jacobian_arithmetic.lower()}"] = \
+            parity_full_size(o, U, R_main, J_main)
+        if alt is not None:
+            rr, jj = parity_full_size(o, U, alt["R"], alt["J"])
+            parity["J_err_over_scale_fp64"] = jj
+            parity["R_identical_across_arithmetic"] = bool(np.array_equal(alt["R"], R_main))
+        parity["bars"] = {"R": 1e-12, "J": 1e-10}
+        cpu_v, cores, n_cpu, cpu_s = cpu_baseline(o, U, budget_s=args.cpu_budget)
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -342,9 +398,13 @@ def run_gpu(args, rank, world, local_rank):
                              "sample": f"{n_cpu} full F+J evaluations ({cpu_s:.1f} s) of the same workload"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * nc,
                     "d2h_bytes_per_step": 8 * (nc + nnz), "steps": e2e_steps},
-            "gpu_launches": args.steps * t.launches_per_evaluation(),
+            "gpu_launches": args.steps * launches,
+            "parity_full_size": parity,
             "clocks": clk.summary(),
         }
+        if alt is not None:
+            out["fp64_jacobian"] = {"value": alt["value"], "unit": UNIT, "ms_per_step": alt["ms_per_step"],
+                                    "note": "same device loop with -tdy_jacobian_arithmetic FP64"}
         print(json.dumps(out), flush=True)
     if dist:
         dist.barrier()
