@@ -72,6 +72,15 @@ TDyErrorCode TDyFinalize(void);
 TDyErrorCode TDyOptionsInsertString(const char *options);
 TDyErrorCode TDyOptionsClear(void);
 const char *TDyGetErrorMessage(void);
+/* Queries of the same options database, standing in for PetscOptionsGetReal,
+ * PetscOptionsGetInt, PetscOptionsGetString and PetscOptionsHasName (used by
+ * the reference's driver, src/tdyti.c:28-44, and its demos). *set is 1 when
+ * the option is present; the value is left unchanged otherwise. A malformed
+ * number returns TDY_ERR_ARG_WRONG. */
+TDyErrorCode TDyOptionsGetReal(const char *name, double *value, int *set);
+TDyErrorCode TDyOptionsGetInt(const char *name, int *value, int *set);
+TDyErrorCode TDyOptionsGetString(const char *name, char *value, int len, int *set);
+TDyErrorCode TDyOptionsHasName(const char *name, int *set);
 
 /* Lifecycle: include/tdycore.h:137-143 (TDyCreate ... TDyDestroy).
  * comm is accepted for signature compatibility and must describe a single
@@ -166,6 +175,14 @@ TDyErrorCode TDySetDtimeForSNESSolver(TDy tdy, double dt);                    /*
 TDyErrorCode TDySetPreviousSolutionForSNESSolver(TDy tdy, const double *U);   /* include/tdycore.h:240 */
 TDyErrorCode TDyPreSolveSNESSolver(TDy tdy);                                 /* src/tdycore.c:2074 */
 TDyErrorCode TDyPostSolve(TDy tdy, const double *U);                         /* src/tdycore.c:2056 */
+/* TDyOutputRegression (src/tdycore.c:1564, src/tdyregression.c:8-250): when
+ * -tdy_regression_test was given to TDySetFromOptions, writes
+ * "<-tdy_regression_test_filename>.regression" with the max, min and mean of
+ * U and U at -tdy_regression_test_num_cells_per_process (default 2) cells
+ * spaced floor(ncells / count) apart, in the reference's text format; a no-op
+ * otherwise. TDySetup fails with TDY_ERR_USER when -tdy_regression_test is
+ * set without a filename, as TDyRegressionInitialize does. */
+TDyErrorCode TDyOutputRegression(TDy tdy, const double *U);
 /* TDyMPFAOSNESFunction (tdympfao_snes.c:67): R[ncells] from U[ncells]. */
 TDyErrorCode TDyMPFAOSNESFunction(TDy tdy, const double *U, double *R);
 /* TDyMPFAOSNESJacobian (tdympfao_snes.c:143): J values in pattern order. */

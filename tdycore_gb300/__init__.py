@@ -77,6 +77,11 @@ lib.TDyGetErrorMessage.argtypes = []
 _sig("TDyInit", c_int, c_void_p)
 _sig("TDyOptionsInsertString", c_char_p)
 _sig("TDyOptionsClear")
+_sig("TDyOptionsGetReal", c_char_p, _dp, _ip)
+_sig("TDyOptionsGetInt", c_char_p, _ip, _ip)
+_sig("TDyOptionsGetString", c_char_p, c_char_p, c_int, _ip)
+_sig("TDyOptionsHasName", c_char_p, _ip)
+_sig("TDyOutputRegression", c_void_p, _dp)
 _sig("TDyCreate", c_void_p, POINTER(c_void_p))
 _sig("TDyDestroy", POINTER(c_void_p))
 _sig("TDySetMode", c_void_p, c_int)
@@ -180,6 +185,31 @@ def options_insert(options: str) -> None:
 
 def options_clear() -> None:
     check(lib.TDyOptionsClear(), "TDyOptionsClear")
+
+
+def options_get_real(name: str, default=None):
+    """PetscOptionsGetReal analogue: the option's value, or ``default``."""
+    v, f = c_double(), c_int()
+    check(lib.TDyOptionsGetReal(name.encode(), byref(v), byref(f)), "TDyOptionsGetReal")
+    return v.value if f.value else default
+
+
+def options_get_int(name: str, default=None):
+    v, f = c_int(), c_int()
+    check(lib.TDyOptionsGetInt(name.encode(), byref(v), byref(f)), "TDyOptionsGetInt")
+    return v.value if f.value else default
+
+
+def options_get_string(name: str, default=None):
+    buf, f = ctypes.create_string_buffer(4096), c_int()
+    check(lib.TDyOptionsGetString(name.encode(), buf, 4096, byref(f)), "TDyOptionsGetString")
+    return buf.value.decode() if f.value else default
+
+
+def options_has_name(name: str) -> bool:
+    f = c_int()
+    check(lib.TDyOptionsHasName(name.encode(), byref(f)), "TDyOptionsHasName")
+    return bool(f.value)
 
 
 class TDy:
@@ -418,9 +448,22 @@ class TDy:
         check(lib.TDySetDtimeForSNESSolver(self._h, dt), "TDySetDtimeForSNESSolver")
 
     def presolve(self, U_prev):
+        """TDySetPreviousSolutionForSNESSolver + TDyPreSolveSNESSolver."""
+        self.set_previous_solution(U_prev)
+        self.presolve_current()
+
+    def set_previous_solution(self, U_prev):
         u = _f64(U_prev, self.ncells)
         check(lib.TDySetPreviousSolutionForSNESSolver(self._h, _as_dp(u)), "TDySetPreviousSolutionForSNESSolver")
+
+    def presolve_current(self):
+        """TDyPreSolveSNESSolver: accumulation at the stored previous solution."""
         check(lib.TDyPreSolveSNESSolver(self._h), "TDyPreSolveSNESSolver")
+
+    def post_solve(self, U):
+        """TDyPostSolve: U becomes the previous solution."""
+        u = _f64(U, self.ncells)
+        check(lib.TDyPostSolve(self._h, _as_dp(u)), "TDyPostSolve")
 
     def snes_function(self, U):
         u = _f64(U, self.ncells)
@@ -512,6 +555,12 @@ class TDy:
         calls = (c_longlong * 8)()
         check(lib.TDyGetTimers(self._h, byref(n), names, ms, calls), "TDyGetTimers")
         return {names[i].decode(): (ms[i], calls[i]) for i in range(n.value)}
+
+    def output_regression(self, U):
+        """TDyOutputRegression: writes <filename>.regression when
+        -tdy_regression_test is set."""
+        u = _f64(U, self.ncells)
+        check(lib.TDyOutputRegression(self._h, _as_dp(u)), "TDyOutputRegression")
 
     # diagnostics ------------------------------------------------------------
     def update_state(self, U):

@@ -64,6 +64,16 @@ static int opt_real(const char *name, double *v) {
   return 0;
 }
 
+static int opt_int(const char *name, int *v) {
+  std::string s;
+  if (!opt_find(name, &s)) return 0;
+  char *end = nullptr;
+  long x = strtol(s.c_str(), &end, 10);
+  if (s.empty() || (end && *end)) return set_error(TDY_ERR_ARG_WRONG, "option %s expects an integer, got '%s'", name, s.c_str());
+  *v = (int)x;
+  return 0;
+}
+
 static int opt_enum(const char *name, const char *const *names, int n, int *v) {
   std::string s;
   if (!opt_find(name, &s)) return 0;
@@ -220,6 +230,35 @@ TDyErrorCode TDyOptionsInsertString(const char *options) {
 }
 TDyErrorCode TDyOptionsClear(void) { return TDyFinalize(); }
 
+TDyErrorCode TDyOptionsGetReal(const char *name, double *value, int *set) {
+  if (!name || !value) return set_error(TDY_ERR_ARG_NULL, "TDyOptionsGetReal: null argument");
+  const int present = opt_find(name, nullptr) ? 1 : 0;
+  if (set) *set = present;
+  return present ? opt_real(name, value) : 0;
+}
+TDyErrorCode TDyOptionsGetInt(const char *name, int *value, int *set) {
+  if (!name || !value) return set_error(TDY_ERR_ARG_NULL, "TDyOptionsGetInt: null argument");
+  const int present = opt_find(name, nullptr) ? 1 : 0;
+  if (set) *set = present;
+  return present ? opt_int(name, value) : 0;
+}
+TDyErrorCode TDyOptionsGetString(const char *name, char *value, int len, int *set) {
+  if (!name || !value || len <= 0) return set_error(TDY_ERR_ARG_NULL, "TDyOptionsGetString: null argument");
+  std::string s;
+  const bool present = opt_find(name, &s);
+  if (set) *set = present ? 1 : 0;
+  if (present) {
+    if ((int)s.size() >= len) return set_error(TDY_ERR_ARG_OUTOFRANGE, "option %s: value longer than %d", name, len - 1);
+    memcpy(value, s.c_str(), s.size() + 1);
+  }
+  return 0;
+}
+TDyErrorCode TDyOptionsHasName(const char *name, int *set) {
+  if (!name || !set) return set_error(TDY_ERR_ARG_NULL, "TDyOptionsHasName: null argument");
+  *set = opt_find(name, nullptr) ? 1 : 0;
+  return 0;
+}
+
 TDyErrorCode TDyCreate(void *comm, TDy *tdy) {
   (void)comm;
   if (!tdy) return set_error(TDY_ERR_ARG_NULL, "TDyCreate: null output pointer");
@@ -272,6 +311,13 @@ TDyErrorCode TDySetFromOptions(TDy tdy) {
   if ((ierr = opt_enum("-tdy_mpfao_boundary_condition_type", bct, 3, &o.bc_type))) return ierr;
   // extension: arithmetic of the Jacobian products (FP64 residual either way)
   if ((ierr = opt_enum("-tdy_jacobian_arithmetic", jarith, 2, &o.jacobian_arithmetic))) return ierr;
+  // regression output (src/tdycore.c:617, src/tdyregression.c:33-45)
+  if (opt_find("-tdy_regression_test", nullptr)) o.regression_testing = true;
+  if ((ierr = opt_int("-tdy_regression_test_num_cells_per_process", &o.regression_num_cells))) return ierr;
+  {
+    std::string fn;
+    if (opt_find("-tdy_regression_test_filename", &fn)) o.regression_filename = fn;
+  }
   double pbc;
   if (opt_find("-tdy_pressure_bc_value", nullptr)) {
     if ((ierr = opt_real("-tdy_pressure_bc_value", &pbc))) return ierr;
@@ -680,6 +726,9 @@ static int setup_host(TDy tdy) {
   if (!(tdy->flags & TDY_FLAG_OPTIONS)) return set_error(TDY_ERR_USER, "You must call TDySetFromOptions before TDySetup()");
   if (tdy->is_setup) return set_error(TDY_ERR_USER, "TDySetup called twice");
   if (!tdy->mesh_in.set) return set_error(TDY_ERR_USER, "no mesh: call TDySetBoxMesh or TDySetExtrudedMesh before TDySetup");
+  // TDyRegressionInitialize (src/tdyregression.c:38-45)
+  if (tdy->opt.regression_testing && tdy->opt.regression_filename.empty())
+    return set_error(TDY_ERR_USER, "Need to specify a regression filename via -tdy_regression_test_filename");
   int ierr;
   if ((ierr = build_extruded_mesh(tdy->mesh_in, tdy->mesh))) return ierr;
   if ((ierr = build_materials(tdy))) return ierr;
@@ -847,6 +896,36 @@ TDyErrorCode TDyPreSolveSNESSolver(TDy tdy) {
   return device_presolve_host(tdy, tdy->U_prev.data());
 }
 TDyErrorCode TDyPostSolve(TDy tdy, const double *U) { return TDySetPreviousSolutionForSNESSolver(tdy, U); }
+
+// TDyRegressionInitialize + TDyRegressionOutput (src/tdyregression.c:8-250)
+// for one process: cells c * floor(n / count), c < count (count capped at n);
+// mean = sum / n with the sum taken in cell order.
+TDyErrorCode TDyOutputRegression(TDy tdy, const double *U) {
+  TDY_CHECK_HANDLE(tdy);
+  TDY_CHECK_SETUP(tdy);
+  if (!tdy->opt.regression_testing) return 0;
+  if (!U) return set_error(TDY_ERR_ARG_NULL, "TDyOutputRegression: null array");
+  const int n = tdy->mesh.nc;
+  int count = tdy->opt.regression_num_cells;
+  if (n < count) count = n;
+  const int inc = count > 0 ? n / count : 0;
+  double mx = U[0], mn = U[0], sum = 0.0;
+  for (int i = 0; i < n; i++) {
+    mx = U[i] > mx ? U[i] : mx;
+    mn = U[i] < mn ? U[i] : mn;
+    sum += U[i];
+  }
+  const std::string fname = tdy->opt.regression_filename + ".regression";
+  FILE *fp = fopen(fname.c_str(), "w");
+  if (!fp) return set_error(TDY_ERR_USER, "Unable to write regression file %s", fname.c_str());
+  fprintf(fp, "-- PRESSURE: Liquid Pressure --\n");
+  fprintf(fp, "      Max: %21.13e\n", mx);
+  fprintf(fp, "      Min: %21.13e\n", mn);
+  fprintf(fp, "     Mean: %21.13e\n", sum / n);
+  for (int c = 0; c < count; c++) fprintf(fp, "%9d: %21.13e\n", c * inc, U[c * inc]);
+  fclose(fp);
+  return 0;
+}
 
 TDyErrorCode TDyMPFAOSNESFunction(TDy tdy, const double *U, double *R) {
   TDY_CHECK_HANDLE(tdy);

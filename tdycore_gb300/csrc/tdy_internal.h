@@ -47,6 +47,10 @@ struct Options {
   double pressure_bc_value = 0.0;
   // arithmetic of the Jacobian products w*T at interior hexahedral vertices
   int jacobian_arithmetic = JACOBIAN_DOUBLE_FLOAT;
+  // regression output (src/tdyregression.c)
+  bool regression_testing = false;
+  std::string regression_filename;
+  int regression_num_cells = 2;
 };
 
 // How a per-cell property is specified by the user.

@@ -6,8 +6,6 @@ else runs on the CPU.  The oracle (oracle/) is the checker for parity tests.
 import sys
 from pathlib import Path
 
-import pytest
-
 ROOT = Path(__file__).resolve().parents[1]
 if str(ROOT) not in sys.path:
     sys.path.insert(0, str(ROOT))
@@ -15,11 +13,8 @@ if str(ROOT) not in sys.path:
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA device (GB300) and the built CUDA library")
-
-
-@pytest.fixture(scope="session", autouse=True)
-def _built_libraries():
-    """Build the product library and the oracle once per session (no-op when up to date)."""
+    # Build the product library and the oracle before test modules are
+    # collected (they import the package); a no-op when up to date.
     import __graft_entry__
 
     __graft_entry__.build()

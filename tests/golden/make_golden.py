@@ -7,6 +7,7 @@ condition of the richards driver problem from a TDycore checkout, and writes
 
     python tests/golden/make_golden.py /path/to/TDycore
 """
+import base64
 import json
 import struct
 import sys
@@ -52,7 +53,12 @@ def main(ref):
     data = {"source": "TDycore regression gold files", "cases": {}}
     for name, rel in CASES.items():
         data["cases"][name] = {"file": rel, **parse_gold((ref / rel).read_text())}
-    data["richards_prob1_ic"] = read_petsc_vec(ref / "demo/richards/richards_driver_snes_prob1_3x3x3_random.vec")
+    vec = ref / "demo/richards/richards_driver_snes_prob1_3x3x3_random.vec"
+    data["richards_prob1_ic"] = read_petsc_vec(vec)
+    # the file itself (80 bytes), for the PETSc-binary reader test
+    data["richards_prob1_ic_petsc_binary_b64"] = base64.b64encode(vec.read_bytes()).decode()
+    # the gold files' text, for the regression-output format test
+    data["gold_text"] = {name: (ref / rel).read_text() for name, rel in CASES.items()}
     out = Path(__file__).resolve().parent / "golden.json"
     out.write_text(json.dumps(data, indent=1, sort_keys=True))
     print("wrote", out)
