@@ -311,6 +311,8 @@ TDyErrorCode TDySetFromOptions(TDy tdy) {
   if ((ierr = opt_enum("-tdy_mpfao_boundary_condition_type", bct, 3, &o.bc_type))) return ierr;
   // extension: arithmetic of the Jacobian products (FP64 residual either way)
   if ((ierr = opt_enum("-tdy_jacobian_arithmetic", jarith, 2, &o.jacobian_arithmetic))) return ierr;
+  // extension: build the interior hexahedral vertices' Trans on the device
+  if (opt_find("-tdy_mpfao_setup_on_device", nullptr)) o.setup_on_device = true;
   // regression output (src/tdycore.c:617, src/tdyregression.c:33-45)
   if (opt_find("-tdy_regression_test", nullptr)) o.regression_testing = true;
   if ((ierr = opt_int("-tdy_regression_test_num_cells_per_process", &o.regression_num_cells))) return ierr;

@@ -24,5 +24,7 @@ int device_set_timers(_p_TDy *t, int on);
 int device_get_timers(_p_TDy *t, int *n, const char **names, double *ms, long long *calls);
 int device_fp64_probe(double *tflops);
 int device_eval_noalloc(_p_TDy *t, const double *dU, double *dR, double *dJ, void *stream);
+// Trans of the canonical vertices into d_Tc (-tdy_mpfao_setup_on_device).
+int device_canon_trans(const _p_TDy *t, const int *d_cellc, const int *d_facec, double *d_Tc);
 
 }  // namespace tdy

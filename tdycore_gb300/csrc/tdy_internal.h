@@ -47,6 +47,8 @@ struct Options {
   double pressure_bc_value = 0.0;
   // arithmetic of the Jacobian products w*T at interior hexahedral vertices
   int jacobian_arithmetic = JACOBIAN_DOUBLE_FLOAT;
+  // interior hexahedral vertices' Trans built on the device (extension)
+  bool setup_on_device = false;
   // regression output (src/tdyregression.c)
   bool regression_testing = false;
   std::string regression_filename;

@@ -818,10 +818,18 @@ int device_setup(_p_TDy *t) {
   UP(a.G, s.gravdis);
   a.nC = s.nC;
   a.nCpad = s.nCpad;
-  UP(a.Tc, s.Tc);
+  if (t->opt.setup_on_device) {
+    double *tc;
+    if ((ierr = dalloc(d, &tc, 96 * (size_t)s.nCpad))) return ierr;
+    a.Tc = tc;
+  } else {
+    UP(a.Tc, s.Tc);
+  }
   a.jac_ff = t->opt.jacobian_arithmetic == JACOBIAN_DOUBLE_FLOAT;
   UP(a.cellc, s.cellc);
   UP(a.facec, s.facec);
+  if (t->opt.setup_on_device && (ierr = device_canon_trans(t, a.cellc, a.facec, const_cast<double *>(a.Tc))))
+    return ierr;
   a.ngen = (int)s.gen_vertex.size();
   UP(a.gen_vertex, s.gen_vertex);
   UP(a.v_row_off, s.v_row_off);

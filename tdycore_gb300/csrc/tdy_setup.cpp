@@ -268,6 +268,41 @@ double face_perm_value(const Mesh &m, const Materials &mat, int method, int f, c
   return (kup * kdn) / (wt_up * kdn + (1.0 - wt_up) * kup);
 }
 
+// Octant layout of a vertex with 8 cells and 12 flux rows: the octant of each
+// local cell from its centroid relative to the vertex (bit 0 x, bit 1 y,
+// bit 2 z) and the canonical row (kCanonUp/kCanonDn) of each vertex row.
+// False when the vertex does not fit: two cells in one octant, a boundary
+// row, a row joining octants that differ in more than one bit, or a row whose
+// first cell is not on the lower side.
+bool canonical_layout(const Mesh &m, int v, const int *cells, const int *lup, const int *ldn,
+                      std::array<int, 8> &oc, std::array<int, 12> &cr) {
+  const double *xv = &m.vx[3 * (size_t)v];
+  oc.fill(-1);
+  cr.fill(-1);
+  int oct_of[8];
+  for (int a = 0; a < 8; a++) {
+    const double *xc = &m.cell_cen[3 * (size_t)cells[a]];
+    int o = (xc[0] > xv[0] ? 1 : 0) | (xc[1] > xv[1] ? 2 : 0) | (xc[2] > xv[2] ? 4 : 0);
+    if (oc[o] >= 0) return false;
+    oc[o] = a;
+    oct_of[a] = o;
+  }
+  for (int r = 0; r < 12; r++) {
+    if (lup[r] < 0 || ldn[r] < 0) return false;
+    int ou = oct_of[lup[r]], od = oct_of[ldn[r]];
+    int diff = ou ^ od;
+    if (diff != 1 && diff != 2 && diff != 4) return false;
+    if (ou & diff) return false;  // the face's first cell must be on the lower side
+    int k = (diff == 1) ? 0 : (diff == 2) ? 1 : 2;
+    int rc = -1;
+    for (int j = 0; j < 4; j++)
+      if (kCanonUp[4 * k + j] == ou) rc = 4 * k + j;
+    if (rc < 0 || cr[rc] >= 0) return false;
+    cr[rc] = r;
+  }
+  return true;
+}
+
 }  // namespace
 
 int mpfao_setup(const Options &opt, const Mesh &m, const Materials &mat, const Boundary &bnd, MPFAOSetup &s) {
@@ -306,6 +341,40 @@ int mpfao_setup(const Options &opt, const Mesh &m, const Materials &mat, const B
       if (!is_neumann(f)) rows.push_back(j);
     }
     const int ncol = nint + nknw;
+    const int nrow = (int)rows.size();
+    auto local_cell = [&](int c) {
+      for (int a = 0; a < nint; a++)
+        if (m.vert_cells[c0 + a] == c) return a;
+      return -1;
+    };
+    // row metadata: face, local up/down cell
+    const size_t rbase = s.row_face.size();
+    for (int r = 0; r < nrow; r++) {
+      int f = m.vert_faces[f0 + rows[r]];
+      s.row_face.push_back(f);
+      s.row_lup.push_back(m.face_cell0[f] >= 0 ? local_cell(m.face_cell0[f]) : -1);
+      s.row_ldn.push_back(m.face_cell1[f] >= 0 ? local_cell(m.face_cell1[f]) : -1);
+    }
+    s.v_nint[v] = nint;
+    s.v_row_off[v + 1] = s.v_row_off[v] + nrow;
+    s.v_col_off[v + 1] = s.v_col_off[v] + ncol;
+    s.v_trans_off[v + 1] = s.v_trans_off[v] + (long long)nrow * ncol;
+    for (int a = 0; a < nint; a++) s.col_ext.push_back(m.vert_cells[c0 + a]);
+    for (int j = 0; j < nfv; j++)
+      if (knw[j] >= 0) s.col_ext.push_back(nc + m.face_bnd[m.vert_faces[f0 + j]]);
+    // interior hexahedral vertices whose Trans the device builds
+    if (opt.setup_on_device && nint == 8 && nknw == 0 && nrow == 12) {
+      std::array<int, 8> oc;
+      std::array<int, 12> cr;
+      if (canonical_layout(m, v, &m.vert_cells[c0], &s.row_lup[rbase], &s.row_ldn[rbase], oc, cr)) {
+        s.trans.insert(s.trans.end(), (size_t)nrow * ncol, 0.0);
+        for (int j = 0; j < nfv; j++) fpos[m.vert_faces[f0 + j]] = -1;
+        s.max_nint = std::max(s.max_nint, nint);
+        s.max_nrow = std::max(s.max_nrow, nrow);
+        s.max_ncol = std::max(s.max_ncol, ncol);
+        continue;
+      }
+    }
     // subcells and their flux coefficients
     // flux_{a,i} = sum_u cu[u] Pi_u + sum_k ck[k] P_D,k + ccell * P_a
     struct Flux {
@@ -334,11 +403,6 @@ int mpfao_setup(const Options &opt, const Mesh &m, const Materials &mat, const B
         }
       }
     }
-    auto local_cell = [&](int c) {
-      for (int a = 0; a < nint; a++)
-        if (m.vert_cells[c0 + a] == c) return a;
-      return -1;
-    };
     auto subcell_face = [&](int a, int f) {
       for (int i = 0; i < 3; i++)
         if (sc[a].face[i] == f) return i;
@@ -370,17 +434,8 @@ int mpfao_setup(const Options &opt, const Mesh &m, const Materials &mat, const B
     if (nunk > 0 && !lu_solve(nunk, ncol, A, B))
       return set_error(TDY_ERR_LIB, "singular interaction-region system at vertex %d", v);
     // B now holds M = A^-1 B.  Trans rows.
-    const int nrow = (int)rows.size();
-    s.v_nint[v] = nint;
-    s.v_row_off[v + 1] = s.v_row_off[v] + nrow;
-    s.v_col_off[v + 1] = s.v_col_off[v] + ncol;
-    s.v_trans_off[v + 1] = s.v_trans_off[v] + (long long)nrow * ncol;
-    for (int a = 0; a < nint; a++) s.col_ext.push_back(m.vert_cells[c0 + a]);
-    for (int j = 0; j < nfv; j++)
-      if (knw[j] >= 0) s.col_ext.push_back(nc + m.face_bnd[m.vert_faces[f0 + j]]);
     for (int r = 0; r < nrow; r++) {
-      int j = rows[r];
-      int f = m.vert_faces[f0 + j];
+      int f = m.vert_faces[f0 + rows[r]];
       int a = (m.face_bnd[f] < 0) ? local_cell(m.face_cell0[f]) : local_cell(m.face_cell1[f]);
       const Flux &F = fl[a][subcell_face(a, f)];
       std::vector<double> t(ncol, 0.0);
@@ -392,9 +447,6 @@ int mpfao_setup(const Options &opt, const Mesh &m, const Materials &mat, const B
       t[a] += F.ccell;
       for (int k = 0; k < nknw; k++) t[nint + k] += F.ck[k];
       s.trans.insert(s.trans.end(), t.begin(), t.end());
-      s.row_face.push_back(f);
-      s.row_lup.push_back(m.face_cell0[f] >= 0 ? local_cell(m.face_cell0[f]) : -1);
-      s.row_ldn.push_back(m.face_cell1[f] >= 0 ? local_cell(m.face_cell1[f]) : -1);
     }
     for (int j = 0; j < nfv; j++) fpos[m.vert_faces[f0 + j]] = -1;
     s.max_nint = std::max(s.max_nint, nint);
@@ -458,47 +510,9 @@ int mpfao_setup(const Options &opt, const Mesh &m, const Materials &mat, const B
     const int r0 = s.v_row_off[v], nrow = s.v_row_off[v + 1] - r0;
     const int c0 = s.v_col_off[v], ncol = s.v_col_off[v + 1] - c0;
     if (nint != 8 || nrow != 12 || ncol != 8) continue;
-    const double *xv = &m.vx[3 * (size_t)v];
     std::array<int, 8> oc;
-    oc.fill(-1);
-    int oct_of[8];
-    bool ok = true;
-    for (int a = 0; a < 8 && ok; a++) {
-      const double *xc = &m.cell_cen[3 * (size_t)s.col_ext[c0 + a]];
-      int o = (xc[0] > xv[0] ? 1 : 0) | (xc[1] > xv[1] ? 2 : 0) | (xc[2] > xv[2] ? 4 : 0);
-      if (oc[o] >= 0) ok = false;
-      oc[o] = a;
-      oct_of[a] = o;
-    }
     std::array<int, 12> cr;
-    cr.fill(-1);
-    for (int r = 0; r < nrow && ok; r++) {
-      int lu = s.row_lup[r0 + r], ld = s.row_ldn[r0 + r];
-      if (lu < 0 || ld < 0) {
-        ok = false;
-        break;
-      }
-      int ou = oct_of[lu], od = oct_of[ld];
-      int diff = ou ^ od;
-      if (diff != 1 && diff != 2 && diff != 4) {
-        ok = false;
-        break;
-      }
-      if (ou & diff) {  // the face's first cell must be on the lower side
-        ok = false;
-        break;
-      }
-      int k = (diff == 1) ? 0 : (diff == 2) ? 1 : 2;
-      int rc = -1;
-      for (int j = 0; j < 4; j++)
-        if (kCanonUp[4 * k + j] == ou) rc = 4 * k + j;
-      if (rc < 0 || cr[rc] >= 0) {
-        ok = false;
-        break;
-      }
-      cr[rc] = r;
-    }
-    if (!ok) continue;
+    if (!canonical_layout(m, v, &s.col_ext[c0], &s.row_lup[r0], &s.row_ldn[r0], oc, cr)) continue;
     canon_idx[v] = (int)s.canon_vertex.size();
     s.canon_vertex.push_back(v);
     octant_col.push_back(oc);
@@ -507,7 +521,7 @@ int mpfao_setup(const Options &opt, const Mesh &m, const Materials &mat, const B
   s.nC = (int)s.canon_vertex.size();
   s.nCpad = ((s.nC + 31) / 32) * 32;
   const long long P = s.nCpad;
-  s.Tc.assign(96 * (size_t)P, 0.0);
+  if (!opt.setup_on_device) s.Tc.assign(96 * (size_t)P, 0.0);  // else built on the device
   s.cellc.assign(8 * (size_t)P, 0);
   s.facec.assign(12 * (size_t)P, 0);
   for (int k = 0; k < s.nC; k++) {
@@ -518,7 +532,8 @@ int mpfao_setup(const Options &opt, const Mesh &m, const Materials &mat, const B
     for (int rc = 0; rc < 12; rc++) {
       const int r = canon_row[k][rc];
       s.facec[rc * P + k] = s.row_face[r0 + r];
-      for (int o = 0; o < 8; o++) s.Tc[(rc * 8 + o) * P + k] = T[r * 8 + octant_col[k][o]];
+      if (!opt.setup_on_device)
+        for (int o = 0; o < 8; o++) s.Tc[(rc * 8 + o) * P + k] = T[r * 8 + octant_col[k][o]];
     }
   }
   // scratch layout

@@ -129,3 +129,36 @@ def test_double_float_jacobian_tracks_fp64(name):
     (Rf, Jf), (Rd, Jd) = runs["DOUBLE_FLOAT"], runs["FP64"]
     assert np.array_equal(Rf, Rd)
     assert_close(Jf, Jd, Jm, 1e-12, f"{name} double-float vs FP64 Jacobian")
+
+
+@pytest.mark.parametrize("name", ["spe10_small", "hydrostatic_box", "tpf_dirichlet", "mixed_curves", "seepage",
+                                  "neumann"])
+def test_device_built_transmissibility(name):
+    """-tdy_mpfao_setup_on_device: the interior hexahedral vertices' Trans is
+    built by the device kernel, eliminating the interaction-region unknowns in
+    another order than the host.  R must meet the usual bar against the oracle
+    on the host-built setup.  For J the bar is taken relative to the larger of
+    the entry's error scale and one FP64 unit (1e-16) of the largest scale in
+    its row: entries that are structural zeros of Trans (orthogonal meshes)
+    hold only rounding noise of the elimination, which two Trans computations
+    produce differently."""
+    parity_cases.EXTRA_OPTIONS = "-tdy_mpfao_setup_on_device"
+    try:
+        t, U, Uprev, Ut = CASES[name]()
+    finally:
+        parity_cases.EXTRA_OPTIONS = ""
+    t.setup()
+    th, _, _, _ = CASES[name]()
+    th.setup(host_only=True)
+    o = Oracle(th.setup_view())
+    assert np.array_equal(t.rowptr, th.rowptr) and np.array_equal(t.colidx, th.colidx)
+    t.set_dtime(DT)
+    t.presolve(Uprev)
+    o.snes_presolve(Uprev, DT)
+    R, J = t.snes_function_jacobian(U)
+    Rr, Rm = o.snes_function(U, with_mag=True)
+    Jr, Jm = o.snes_jacobian(U, with_mag=True)
+    assert_close(R, Rr, Rm, R_TOL, f"{name} SNES residual, device-built Trans")
+    rowmax = np.maximum.reduceat(Jm, t.rowptr[:-1])
+    row_of = np.repeat(np.arange(t.ncells), np.diff(t.rowptr))
+    assert_close(J, Jr, np.maximum(Jm, 1e-16 * rowmax[row_of]), J_TOL, f"{name} SNES Jacobian, device-built Trans")
