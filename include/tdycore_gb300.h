@@ -195,6 +195,26 @@ TDyErrorCode TDyMPFAOIFunction(TDy tdy, double t, const double *U, const double 
 TDyErrorCode TDyMPFAOIJacobian(TDy tdy, double t, const double *U, const double *U_t, double shift, double *J);
 TDyErrorCode TDyMPFAOIFunctionIJacobian(TDy tdy, double t, const double *U, const double *U_t, double shift,
                                         double *R, double *J);
+/* ---------------------------------------------------------------------- */
+/* TS variants with the same flux kernels (TDySetDiscretization MPFA_O_TRANSIENTVAR
+ * or MPFA_O_DAE; src/tdycore.c:1902-1908). */
+/* TDyMPFAOTransientVariable (tdympfao_ts_transientvar.c:13-47): the conserved
+ * variable C = rho * porosity * S * volume per cell. */
+TDyErrorCode TDyMPFAOTransientVariable(TDy tdy, const double *U, double *C);
+/* Extension: dC/dP per cell (d(rho porosity S)/dP * volume). */
+TDyErrorCode TDyMPFAOTransientVariableDerivative(TDy tdy, const double *U, double *dC);
+/* TDyMPFAOIFunction_TransientVariable (tdympfao_ts_transientvar.c:50-101):
+ * R = fluxes + M_t * volume - source * volume, M_t the rate of C. */
+TDyErrorCode TDyMPFAOIFunctionTransientVariable(TDy tdy, double t, const double *U, const double *M_t, double *R);
+/* Extension: the Jacobian of that residual when M_t = shift * C(U) + const
+ * (fluxes + shift * dC/dP on the diagonal), in pattern order.  The reference
+ * registers no IJacobian for this form and lets PETSc difference it. */
+TDyErrorCode TDyMPFAOIJacobianTransientVariable(TDy tdy, double t, const double *U, double shift, double *J);
+/* TDyMPFAOIFunction_DAE (tdympfao_ts_dae.c:13-84): U, U_t and R hold
+ * [P, M] interleaved per cell (2 * ncells values); R_P = M_t * volume -
+ * source * volume + fluxes, R_M = M - rho * porosity * S * volume.  The
+ * reference registers no IJacobian for this form either. */
+TDyErrorCode TDyMPFAOIFunctionDAE(TDy tdy, double t, const double *U, const double *U_t, double *R);
 
 /* Device-pointer variants (HBM-resident operands). R or J may be NULL to
  * skip that output. stream is a cudaStream_t or NULL. */

@@ -60,6 +60,10 @@ def _load():
     lib.oracle_ts_ijacobian.argtypes = [c_void_p, _dp, _dp, c_double, _dp, _dp]
     lib.oracle_snes_function_jacobian_parallel.argtypes = [c_void_p, _dp, _dp, _dp, c_int]
     lib.oracle_get_state.argtypes = [c_void_p, _dp, _dp, _dp]
+    lib.oracle_transient_variable.argtypes = [c_void_p, _dp, _dp, _dp]
+    lib.oracle_tv_ifunction.argtypes = [c_void_p, _dp, _dp, _dp, _dp]
+    lib.oracle_tv_ijacobian.argtypes = [c_void_p, _dp, c_double, _dp, _dp]
+    lib.oracle_dae_ifunction.argtypes = [c_void_p, _dp, _dp, _dp, _dp]
     return lib
 
 
@@ -151,6 +155,36 @@ class Oracle:
         M = np.empty(self.nnz) if with_mag else None
         lib().oracle_ts_ijacobian(self._ctx, _p(u), _p(ut), shift, _p(J), _p(M) if with_mag else None)
         return (J, M) if with_mag else J
+
+    def transient_variable(self, U, with_derivative=False):
+        u = np.ascontiguousarray(U, dtype=np.float64)
+        C = np.empty(self.nc)
+        dC = np.empty(self.nc) if with_derivative else None
+        lib().oracle_transient_variable(self._ctx, _p(u), _p(C), _p(dC) if with_derivative else None)
+        return (C, dC) if with_derivative else C
+
+    def tv_ifunction(self, U, Mdot, with_mag=False):
+        u = np.ascontiguousarray(U, dtype=np.float64)
+        md = np.ascontiguousarray(Mdot, dtype=np.float64)
+        R = np.empty(self.nc)
+        M = np.empty(self.nc) if with_mag else None
+        lib().oracle_tv_ifunction(self._ctx, _p(u), _p(md), _p(R), _p(M) if with_mag else None)
+        return (R, M) if with_mag else R
+
+    def tv_ijacobian(self, U, shift, with_mag=False):
+        u = np.ascontiguousarray(U, dtype=np.float64)
+        J = np.empty(self.nnz)
+        M = np.empty(self.nnz) if with_mag else None
+        lib().oracle_tv_ijacobian(self._ctx, _p(u), shift, _p(J), _p(M) if with_mag else None)
+        return (J, M) if with_mag else J
+
+    def dae_ifunction(self, U, Ut, with_mag=False):
+        u = np.ascontiguousarray(U, dtype=np.float64)
+        ut = np.ascontiguousarray(Ut, dtype=np.float64)
+        R = np.empty(2 * self.nc)
+        M = np.empty(2 * self.nc) if with_mag else None
+        lib().oracle_dae_ifunction(self._ctx, _p(u), _p(ut), _p(R), _p(M) if with_mag else None)
+        return (R, M) if with_mag else R
 
     def snes_function_jacobian_parallel(self, U, nthreads=0):
         u = np.ascontiguousarray(U, dtype=np.float64)

@@ -606,6 +606,65 @@ void oracle_ts_ifunction(OracleCtx *c, const double *U, const double *Ut, double
   }
 }
 
+/* dmass/dP of one cell, mass = rho * porosity * S (tdympfao_ts.c:470-480) */
+static inline double dmass_dP_cell(OracleCtx *c, int i) {
+  const double dporosity_dP = 0.0;
+  return c->rho[i] * dporosity_dP * c->S[i] + c->drho_dP[i] * c->in.porosity[i] * c->S[i] +
+         c->rho[i] * c->in.porosity[i] * c->dS_dP[i];
+}
+
+/* TDyMPFAOTransientVariable (tdympfao_ts_transientvar.c:13-47): C = rho phi S V;
+ * dC (optional) = d(rho phi S)/dP V. */
+void oracle_transient_variable(OracleCtx *c, const double *U, double *C, double *dC) {
+  const OracleInput *in = &c->in;
+  update_state_range(c, U, 0, c->nc);
+  for (int i = 0; i < c->nc; i++) {
+    C[i] = c->rho[i] * in->porosity[i] * c->S[i] * in->volume[i];
+    if (dC) dC[i] = dmass_dP_cell(c, i) * in->volume[i];
+  }
+}
+
+/* TDyMPFAOIFunction_TransientVariable (tdympfao_ts_transientvar.c:50-101):
+ * R = fluxes + dM/dt V - source V. */
+void oracle_tv_ifunction(OracleCtx *c, const double *U, const double *Mdot, double *R, double *Rmag) {
+  const OracleInput *in = &c->in;
+  memset(R, 0, sizeof(double) * c->nc);
+  if (Rmag) memset(Rmag, 0, sizeof(double) * c->nc);
+  update_all(c, U);
+  for (int v = 0; v < c->nv; v++) ifunction_vertex(c, v, R, Rmag);
+  for (int i = 0; i < c->nc; i++) {
+    double t1 = Mdot[i] * in->volume[i], t2 = in->source_sink[i] * in->volume[i];
+    R[i] += t1;
+    R[i] -= t2;
+    if (Rmag) Rmag[i] += fabs(t1) + fabs(t2);
+  }
+}
+
+/* TDyMPFAOIFunction_DAE (tdympfao_ts_dae.c:13-84): U, U_t and R hold [P, M]
+ * interleaved per cell; R_P = M_t V - source V + fluxes, R_M = M - rho phi S V. */
+void oracle_dae_ifunction(OracleCtx *c, const double *U, const double *Ut, double *R, double *Rmag) {
+  const OracleInput *in = &c->in;
+  const int n = c->nc;
+  double *P = (double *)malloc(sizeof(double) * n), *rp = (double *)calloc(n, sizeof(double));
+  double *rpm = Rmag ? (double *)calloc(n, sizeof(double)) : NULL;
+  for (int i = 0; i < n; i++) P[i] = U[2 * i];
+  update_all(c, P);
+  for (int v = 0; v < c->nv; v++) ifunction_vertex(c, v, rp, rpm);
+  for (int i = 0; i < n; i++) {
+    const double vol = in->volume[i];
+    R[2 * i] = Ut[2 * i + 1] * vol - in->source_sink[i] * vol + rp[i];
+    const double mass = c->rho[i] * in->porosity[i] * c->S[i] * vol;
+    R[2 * i + 1] = U[2 * i + 1] - mass;
+    if (Rmag) {
+      Rmag[2 * i] = fabs(Ut[2 * i + 1] * vol) + fabs(in->source_sink[i] * vol) + rpm[i];
+      Rmag[2 * i + 1] = fabs(U[2 * i + 1]) + fabs(mass);
+    }
+  }
+  free(P);
+  free(rp);
+  free(rpm);
+}
+
 /* ---------------------------------------------------------------------------
  * Jacobian */
 
@@ -772,6 +831,22 @@ void oracle_ts_ijacobian(OracleCtx *c, const double *U, const double *Ut, double
                          d2S * rho * poro + dS * drho_dP * poro + dS * rho * dporosity_dP);
     double value = (shift * dmass_dP + d2mass_dP2 * Ut[icell]) * in->volume[icell];
     mat_add_row(c, J, Jmag, icell, 1, &icell, &value, NULL);
+  }
+}
+
+/* Jacobian of the transient-variable residual R(U, shift C(U) + const):
+ * fluxes plus shift dC/dP on the diagonal.  The reference registers no
+ * IJacobian for this form (src/tdycore.c:1956-1958) and leaves it to PETSc's
+ * finite differences; this is the exact derivative of the same residual. */
+void oracle_tv_ijacobian(OracleCtx *c, const double *U, double shift, double *J, double *Jmag) {
+  const OracleInput *in = &c->in;
+  memset(J, 0, sizeof(double) * c->nnz);
+  if (Jmag) memset(Jmag, 0, sizeof(double) * c->nnz);
+  update_all(c, U);
+  for (int v = 0; v < c->nv; v++) ijacobian_vertex(c, v, J, Jmag);
+  for (int i = 0; i < c->nc; i++) {
+    double value = shift * dmass_dP_cell(c, i) * in->volume[i];
+    mat_add_row(c, J, Jmag, i, 1, &i, &value, NULL);
   }
 }
 

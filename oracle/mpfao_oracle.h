@@ -68,6 +68,11 @@ void oracle_snes_jacobian(OracleCtx *ctx, const double *U, double *J, double *Jm
 /* TDyMPFAOIFunction / TDyMPFAOIJacobian (tdympfao_ts.c:153-227, 520-561) */
 void oracle_ts_ifunction(OracleCtx *ctx, const double *U, const double *Ut, double *R, double *Rmag);
 void oracle_ts_ijacobian(OracleCtx *ctx, const double *U, const double *Ut, double shift, double *J, double *Jmag);
+/* transient-variable and DAE forms (tdympfao_ts_transientvar.c, tdympfao_ts_dae.c) */
+void oracle_transient_variable(OracleCtx *ctx, const double *U, double *C, double *dC);
+void oracle_tv_ifunction(OracleCtx *ctx, const double *U, const double *Mdot, double *R, double *Rmag);
+void oracle_tv_ijacobian(OracleCtx *ctx, const double *U, double shift, double *J, double *Jmag);
+void oracle_dae_ifunction(OracleCtx *ctx, const double *U, const double *Ut, double *R, double *Rmag);
 /* Fused SNES F+J over all host threads, vertices processed by colour (used
  * for the CPU baseline timing; same arithmetic, different summation order). */
 void oracle_snes_function_jacobian_parallel(OracleCtx *ctx, const double *U, double *R, double *J, int nthreads);

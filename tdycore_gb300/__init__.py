@@ -129,6 +129,11 @@ _sig("TDyMPFAOSNESFunctionJacobian", c_void_p, _dp, _dp, _dp)
 _sig("TDyMPFAOIFunction", c_void_p, c_double, _dp, _dp, _dp)
 _sig("TDyMPFAOIJacobian", c_void_p, c_double, _dp, _dp, c_double, _dp)
 _sig("TDyMPFAOIFunctionIJacobian", c_void_p, c_double, _dp, _dp, c_double, _dp, _dp)
+_sig("TDyMPFAOTransientVariable", c_void_p, _dp, _dp)
+_sig("TDyMPFAOTransientVariableDerivative", c_void_p, _dp, _dp)
+_sig("TDyMPFAOIFunctionTransientVariable", c_void_p, c_double, _dp, _dp, _dp)
+_sig("TDyMPFAOIJacobianTransientVariable", c_void_p, c_double, _dp, c_double, _dp)
+_sig("TDyMPFAOIFunctionDAE", c_void_p, c_double, _dp, _dp, _dp)
 _sig("TDyMPFAOSNESFunctionJacobianDevice", c_void_p, c_void_p, c_void_p, c_void_p, c_void_p)
 _sig("TDyMPFAOIFunctionIJacobianDevice", c_void_p, c_double, c_void_p, c_void_p, c_double, c_void_p, c_void_p,
      c_void_p)
@@ -218,6 +223,7 @@ class TDy:
     def __init__(self):
         self._h = c_void_p()
         check(lib.TDyCreate(None, byref(self._h)), "TDyCreate")
+        self.discretization = MPFA_O
         self._keep = []  # ctypes callbacks must outlive the handle
         self.ncells = 0
         self.nnz = 0
@@ -229,6 +235,7 @@ class TDy:
 
     def set_discretization(self, disc=MPFA_O):
         check(lib.TDySetDiscretization(self._h, disc), "TDySetDiscretization")
+        self.discretization = disc
         return self
 
     def set_from_options(self):
@@ -510,6 +517,38 @@ class TDy:
         check(lib.TDyMPFAOIFunctionIJacobian(self._h, t, _as_dp(u), _as_dp(ut), shift, _as_dp(R), _as_dp(J)),
               "TDyMPFAOIFunctionIJacobian")
         return R, J
+
+    # transient-variable and DAE forms ----------------------------------------
+    def transient_variable(self, U, with_derivative=False):
+        u = _f64(U, self.ncells)
+        C = np.empty(self.ncells)
+        check(lib.TDyMPFAOTransientVariable(self._h, _as_dp(u), _as_dp(C)), "TDyMPFAOTransientVariable")
+        if not with_derivative:
+            return C
+        dC = np.empty(self.ncells)
+        check(lib.TDyMPFAOTransientVariableDerivative(self._h, _as_dp(u), _as_dp(dC)),
+              "TDyMPFAOTransientVariableDerivative")
+        return C, dC
+
+    def tv_ifunction(self, t, U, M_t):
+        u, m = _f64(U, self.ncells), _f64(M_t, self.ncells)
+        R = np.empty(self.ncells)
+        check(lib.TDyMPFAOIFunctionTransientVariable(self._h, t, _as_dp(u), _as_dp(m), _as_dp(R)),
+              "TDyMPFAOIFunctionTransientVariable")
+        return R
+
+    def tv_ijacobian(self, t, U, shift):
+        u = _f64(U, self.ncells)
+        J = np.empty(self.nnz)
+        check(lib.TDyMPFAOIJacobianTransientVariable(self._h, t, _as_dp(u), shift, _as_dp(J)),
+              "TDyMPFAOIJacobianTransientVariable")
+        return J
+
+    def dae_ifunction(self, t, U, U_t):
+        u, ut = _f64(U, 2 * self.ncells), _f64(U_t, 2 * self.ncells)
+        R = np.empty(2 * self.ncells)
+        check(lib.TDyMPFAOIFunctionDAE(self._h, t, _as_dp(u), _as_dp(ut), _as_dp(R)), "TDyMPFAOIFunctionDAE")
+        return R
 
     # device-pointer forms (torch tensors or raw pointers) -------------------
     @staticmethod

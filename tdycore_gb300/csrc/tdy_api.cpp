@@ -278,7 +278,9 @@ TDyErrorCode TDySetMode(TDy tdy, TDyMode mode) {
 TDyErrorCode TDySetDiscretization(TDy tdy, TDyDiscretization d) {
   TDY_CHECK_HANDLE(tdy);
   if (!(tdy->flags & TDY_FLAG_MODE)) return set_error(TDY_ERR_USER, "You must call TDySetMode before TDySetDiscretization");
-  if (d != MPFA_O) return set_error(TDY_ERR_SUP, "only the MPFA_O discretization is provided on this path");
+  if (d != MPFA_O && d != MPFA_O_DAE && d != MPFA_O_TRANSIENTVAR)
+    return set_error(TDY_ERR_SUP, "only the MPFA_O discretizations (MPFA_O, MPFA_O_DAE, MPFA_O_TRANSIENTVAR) are "
+                                  "provided on this path");
   tdy->discretization = d;
   tdy->flags |= TDY_FLAG_DISC;
   return 0;
@@ -959,6 +961,38 @@ TDyErrorCode TDyMPFAOIJacobian(TDy tdy, double t, const double *U, const double 
   if (!U || !U_t || !J) return set_error(TDY_ERR_ARG_NULL, "null array");
   return device_eval_host(tdy, FORM_TS, t, U, U_t, shift, nullptr, J);
 }
+TDyErrorCode TDyMPFAOTransientVariable(TDy tdy, const double *U, double *C) {
+  TDY_CHECK_HANDLE(tdy);
+  TDY_CHECK_DEVICE(tdy);
+  if (!U || !C) return set_error(TDY_ERR_ARG_NULL, "null array");
+  return device_transient_variable_host(tdy, U, C, nullptr);
+}
+TDyErrorCode TDyMPFAOTransientVariableDerivative(TDy tdy, const double *U, double *dC) {
+  TDY_CHECK_HANDLE(tdy);
+  TDY_CHECK_DEVICE(tdy);
+  if (!U || !dC) return set_error(TDY_ERR_ARG_NULL, "null array");
+  return device_transient_variable_host(tdy, U, nullptr, dC);
+}
+TDyErrorCode TDyMPFAOIFunctionTransientVariable(TDy tdy, double t, const double *U, const double *M_t, double *R) {
+  TDY_CHECK_HANDLE(tdy);
+  TDY_CHECK_DEVICE(tdy);
+  if (!U || !M_t || !R) return set_error(TDY_ERR_ARG_NULL, "null array");
+  return device_eval_host(tdy, FORM_TV, t, U, M_t, 0.0, R, nullptr);
+}
+TDyErrorCode TDyMPFAOIJacobianTransientVariable(TDy tdy, double t, const double *U, double shift, double *J) {
+  TDY_CHECK_HANDLE(tdy);
+  TDY_CHECK_DEVICE(tdy);
+  if (!U || !J) return set_error(TDY_ERR_ARG_NULL, "null array");
+  // the diagonal term does not depend on M_t; pass U as a placeholder rate
+  return device_eval_host(tdy, FORM_TV, t, U, U, shift, nullptr, J);
+}
+TDyErrorCode TDyMPFAOIFunctionDAE(TDy tdy, double t, const double *U, const double *U_t, double *R) {
+  TDY_CHECK_HANDLE(tdy);
+  TDY_CHECK_DEVICE(tdy);
+  if (!U || !U_t || !R) return set_error(TDY_ERR_ARG_NULL, "null array");
+  return device_eval_dae_host(tdy, t, U, U_t, R);
+}
+
 TDyErrorCode TDyMPFAOIFunctionIJacobian(TDy tdy, double t, const double *U, const double *U_t, double shift, double *R,
                                         double *J) {
   TDY_CHECK_HANDLE(tdy);

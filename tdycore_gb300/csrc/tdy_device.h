@@ -5,7 +5,9 @@
 
 namespace tdy {
 
-enum { FORM_SNES = 0, FORM_TS = 1 };
+// accumulation terms: SNES backward Euler, TS (dm/dP U_t), TS with the mass
+// as transient variable (M_t given)
+enum { FORM_SNES = 0, FORM_TS = 1, FORM_TV = 2 };
 
 int device_setup(_p_TDy *t);
 void device_destroy(_p_TDy *t);
@@ -24,6 +26,10 @@ int device_set_timers(_p_TDy *t, int on);
 int device_get_timers(_p_TDy *t, int *n, const char **names, double *ms, long long *calls);
 int device_fp64_probe(double *tflops);
 int device_eval_noalloc(_p_TDy *t, const double *dU, double *dR, double *dJ, void *stream);
+// C = rho phi S V and dC = d(rho phi S)/dP V per cell (either may be null).
+int device_transient_variable_host(_p_TDy *t, const double *U, double *C, double *dC);
+// DAE form: U, U_t, R interleaved [P, M] per cell (2 * ncells values).
+int device_eval_dae_host(_p_TDy *t, double time, const double *U2, const double *Ut2, double *R2);
 // Trans of the canonical vertices into d_Tc (-tdy_mpfao_setup_on_device).
 int device_canon_trans(const _p_TDy *t, const int *d_cellc, const int *d_facec, double *d_Tc);
 

@@ -114,6 +114,7 @@ struct DeviceState {
   std::vector<void *> allocs;
   double *dU = nullptr, *dUt = nullptr, *dR = nullptr, *dJ = nullptr;
   double *diagS = nullptr, *diagMass = nullptr;
+  double *dae = nullptr;  // DAE form: U, U_t, R interleaved (6 * nc), on first use
   int nnz = 0;
 };
 
@@ -292,6 +293,12 @@ __global__ void __launch_bounds__(256) state_kernel(DevArgs a, int nchunks, int 
       a.acc_a[i] = acc - a.accum_prev[i];
       a.acc_b[i] = a.ss[i];
       a.jdiag[i] = dmass * vol * dtInv;
+    } else if (a.form == FORM_TV) {
+      // TDyMPFAOIFunction_TransientVariable (tdympfao_ts_transientvar.c:89-95):
+      // Ut holds dM/dt; the Jacobian adds shift * dM/dP * V.
+      a.acc_a[i] = a.Ut[i] * vol;
+      a.acc_b[i] = a.ss[i] * vol;
+      a.jdiag[i] = a.shift * dmass * vol;
     } else {
       const double Ut = a.Ut[i];
       const double d2poro = 0.0;
@@ -341,6 +348,40 @@ __global__ void __launch_bounds__(256) presolve_kernel(DevArgs a, const double *
   double rho, drho, d2rho;
   density(a.rho_type, a.Pref - Pc, &rho, &drho, &d2rho);
   accum_prev[i] = rho * a.poro[i] * S * a.vol[i] / a.dt;
+}
+
+// Transient variable (TDyMPFAOTransientVariable, tdympfao_ts_transientvar.c:
+// 13-47): C = rho phi S V, and its pressure derivative.
+__global__ void __launch_bounds__(256) tv_kernel(DevArgs a, const double *U, double *C, double *dC) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.nc) return;
+  const double Sr = a.Sr[i];
+  const double Pc = a.Pref - U[i];
+  double S, dS, d2S;
+  saturation(a.sat_type[i], a.sat_param + 3 * (size_t)i, Sr, Pc, &S, &dS, &d2S);
+  double rho, drho, d2rho;
+  density(a.rho_type, a.Pref - Pc, &rho, &drho, &d2rho);
+  const double poro = a.poro[i], vol = a.vol[i];
+  if (C) C[i] = rho * poro * S * vol;
+  if (dC) dC[i] = (rho * 0.0 * S + drho * poro * S + rho * poro * dS) * vol;
+}
+
+// DAE form (TDyMPFAOIFunction_DAE, tdympfao_ts_dae.c:13-84): split the
+// interleaved [P, M] unknowns, then combine R_P (the transient-variable
+// residual with dM/dt) and R_M = M - rho phi S V.
+__global__ void __launch_bounds__(256) dae_split_kernel(int n, const double *U2, const double *Ut2, double *P,
+                                                        double *Mdot) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  P[i] = U2[2 * i];
+  Mdot[i] = Ut2[2 * i + 1];
+}
+__global__ void __launch_bounds__(256) dae_merge_kernel(int n, const double *U2, const double *Rp, const double *C,
+                                                        double *R2) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  R2[2 * i] = Rp[i];
+  R2[2 * i + 1] = U2[2 * i + 1] - C[i];
 }
 
 // Diagnostics (TDyUpdateDiagnostics_MPFAO, tdympfao.c:2780-2806): saturation
@@ -1069,6 +1110,40 @@ int device_fp64_probe(double *tflops) {
   cudaFree(out);
   double flops = 2.0 * 8.0 * iters * (double)blocks * threads * reps;
   *tflops = flops / (ms * 1e-3) / 1e12;
+  return 0;
+}
+
+int device_transient_variable_host(_p_TDy *t, const double *U, double *C, double *dC) {
+  DeviceState *d = t->dev;
+  const size_t n = (size_t)t->mesh.nc;
+  CUDA_TRY(cudaMemcpyAsync(d->dU, U, sizeof(double) * n, cudaMemcpyHostToDevice, d->stream));
+  tv_kernel<<<nblocks(n, 256), 256, 0, d->stream>>>(d->a, d->dU, C ? d->diagS : nullptr, dC ? d->diagMass : nullptr);
+  CUDA_TRY(cudaGetLastError());
+  if (C) CUDA_TRY(cudaMemcpyAsync(C, d->diagS, sizeof(double) * n, cudaMemcpyDeviceToHost, d->stream));
+  if (dC) CUDA_TRY(cudaMemcpyAsync(dC, d->diagMass, sizeof(double) * n, cudaMemcpyDeviceToHost, d->stream));
+  CUDA_TRY(cudaStreamSynchronize(d->stream));
+  return 0;
+}
+
+int device_eval_dae_host(_p_TDy *t, double time, const double *U2, const double *Ut2, double *R2) {
+  DeviceState *d = t->dev;
+  const int n = t->mesh.nc;
+  if (!d->dae) {  // interleaved buffers, allocated on the first DAE call
+    int ierr;
+    if ((ierr = dalloc(d, &d->dae, 6 * (size_t)n))) return ierr;
+  }
+  double *dU2 = d->dae, *dUt2 = d->dae + 2 * (size_t)n, *dR2 = d->dae + 4 * (size_t)n;
+  CUDA_TRY(cudaMemcpyAsync(dU2, U2, sizeof(double) * 2 * n, cudaMemcpyHostToDevice, d->stream));
+  CUDA_TRY(cudaMemcpyAsync(dUt2, Ut2, sizeof(double) * 2 * n, cudaMemcpyHostToDevice, d->stream));
+  dae_split_kernel<<<nblocks(n, 256), 256, 0, d->stream>>>(n, dU2, dUt2, d->dU, d->dUt);
+  CUDA_TRY(cudaGetLastError());
+  int ierr = device_eval(t, FORM_TV, time, d->dU, d->dUt, 0.0, d->dR, nullptr, d->stream);
+  if (ierr) return ierr;
+  tv_kernel<<<nblocks(n, 256), 256, 0, d->stream>>>(d->a, d->dU, d->diagS, nullptr);
+  dae_merge_kernel<<<nblocks(n, 256), 256, 0, d->stream>>>(n, dU2, d->dR, d->diagS, dR2);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaMemcpyAsync(R2, dR2, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost, d->stream));
+  CUDA_TRY(cudaStreamSynchronize(d->stream));
   return 0;
 }
 

@@ -38,7 +38,7 @@ import numpy as np
 import scipy.sparse as sp
 import scipy.sparse.linalg as spla
 
-from . import options_get_real, options_get_string, options_has_name
+from . import MPFA_O, MPFA_O_DAE, MPFA_O_TRANSIENTVAR, options_get_real, options_get_string, options_has_name
 
 # SNESConvergedReason values (PETSc include/petscsnes.h)
 CONVERGED_FNORM_ABS = 2
@@ -240,6 +240,45 @@ class SNESNewtonLS:
 
 
 # ---------------------------------------------------------------------------
+# Jacobian of the DAE form over interleaved unknowns [P_0, M_0, P_1, M_1, ...]:
+# row 2i holds the flux row of cell i (columns 2j) plus column 2i+1; row 2i+1
+# holds columns 2i and 2i+1.
+def dae_pattern(t):
+    cache = getattr(t, "_dae_pattern", None)
+    if cache is not None:
+        return cache
+    n, rp, ci = t.ncells, t.rowptr, t.colidx
+    counts = np.empty(2 * n, dtype=np.int64)
+    counts[0::2] = np.diff(rp) + 1
+    counts[1::2] = 2
+    rp2 = np.concatenate([[0], np.cumsum(counts)]).astype(np.int32)
+    ci2 = np.empty(rp2[-1], dtype=np.int32)
+    for i in range(n):
+        a = rp2[2 * i]
+        cols = np.concatenate([2 * ci[rp[i]:rp[i + 1]], [2 * i + 1]])
+        ci2[a:a + cols.size] = np.sort(cols)
+        ci2[rp2[2 * i + 1]:rp2[2 * i + 1] + 2] = (2 * i, 2 * i + 1)
+    t._dae_pattern = (rp2, ci2, t.cell_volumes())
+    return t._dae_pattern
+
+
+def dae_values(t, Jflux, dRp_dM, dRm_dP, dRm_dM):
+    n, rp, ci = t.ncells, t.rowptr, t.colidx
+    rp2, ci2, _ = dae_pattern(t)
+    vals = np.empty(rp2[-1])
+    for i in range(n):
+        a, b = rp[i], rp[i + 1]
+        cols = ci[a:b]
+        k = int(np.searchsorted(2 * cols, 2 * i + 1))  # position of column 2i+1 among the sorted row
+        base = rp2[2 * i]
+        vals[base:base + k] = Jflux[a:a + k]
+        vals[base + k] = dRp_dM[i]
+        vals[base + k + 1:base + (b - a) + 1] = Jflux[a + k:b]
+        vals[rp2[2 * i + 1]] = dRm_dP[i]
+        vals[rp2[2 * i + 1] + 1] = dRm_dM[i]
+    return vals
+
+
 def initial_condition(ncells: int, seed: int = 0) -> np.ndarray:
     """TDyRichardsInitialize (src/tdyrichards.c:5-28) from the options."""
     init_file = options_get_string("-tdy_init_file")
@@ -345,16 +384,14 @@ class TimeIntegrator:
                     break
                 self._update_dt(sync_time)
         else:
-            # PETSc TSBEULER, fixed step dt_init, TS_EXACTFINALTIME_MATCHSTEP
+            # PETSc TSBEULER, fixed step dt_init, TS_EXACTFINALTIME_MATCHSTEP,
+            # with the IFunction of the handle's discretization
             tmax = sync_time - self.time
             dt = self.dt_init
             tt = 0.0
             while tmax - tt > 1e-12 * max(1.0, abs(tmax)):
                 h = min(dt, tmax - tt)
-                U0 = self.soln.copy()
-                res = self.snes.solve(lambda x: t.ifunction(self.time + tt + h, x, (x - U0) / h),
-                                      lambda x: t.ijacobian(self.time + tt + h, x, (x - U0) / h, 1.0 / h),
-                                      U0.copy(), t.rowptr, t.colidx)
+                res = self._ts_beuler_step(self.time + tt + h, h)
                 if res.reason < 0:
                     raise RuntimeError(f"TS step failed: SNES reason {res.reason}")
                 self.soln = res.x
@@ -362,8 +399,37 @@ class TimeIntegrator:
                 self.istep += 1
                 self.history.append((self.istep, self.time + tt, h, res.iterations, res.reason))
             self.time += tt
-            t.post_solve(self.soln)
+            dae = getattr(t, "discretization", MPFA_O) == MPFA_O_DAE
+            t.post_solve(self.soln[0::2] if dae else self.soln)
         return self.soln
+
+    def _ts_beuler_step(self, time, h):
+        """One backward-Euler step of the handle's TS form: F(t, U, (U - U_n)/h)
+        = 0 (TDyMPFAOIFunction), its transient-variable form with
+        M_t = (C(U) - C(U_n))/h (TDyMPFAOIFunction_TransientVariable), or the
+        DAE form over interleaved [P, M] (TDyMPFAOIFunction_DAE)."""
+        t = self.tdy
+        U0 = self.soln.copy()
+        disc = getattr(t, "discretization", MPFA_O)
+        if disc == MPFA_O_TRANSIENTVAR:
+            C0 = t.transient_variable(U0)
+            return self.snes.solve(lambda x: t.tv_ifunction(time, x, (t.transient_variable(x) - C0) / h),
+                                   lambda x: t.tv_ijacobian(time, x, 1.0 / h), U0.copy(), t.rowptr, t.colidx)
+        if disc == MPFA_O_DAE:
+            rp, ci, vol = dae_pattern(t)
+            n = t.ncells
+
+            def jac(x):
+                # [dR_P/dP  dR_P/dM; dR_M/dP  dR_M/dM] = [fluxes  V/h; -dC/dP  1]
+                P = x[0::2]
+                Jf = t.tv_ijacobian(time, P, 0.0)
+                _, dC = t.transient_variable(P, with_derivative=True)
+                return dae_values(t, Jf, vol / h, -dC, np.ones(n))
+
+            return self.snes.solve(lambda x: t.dae_ifunction(time, x, (x - U0) / h), jac, U0.copy(), rp, ci)
+        return self.snes.solve(lambda x: t.ifunction(time, x, (x - U0) / h),
+                               lambda x: t.ijacobian(time, x, (x - U0) / h, 1.0 / h), U0.copy(), t.rowptr,
+                               t.colidx)
 
     def output_regression(self):
         """TDyTimeIntegratorOutputRegression: regression file of the previous
