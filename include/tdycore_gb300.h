@@ -109,6 +109,15 @@ TDyErrorCode TDyDestroy(TDy *tdy);
 TDyErrorCode TDySetBoxMesh(TDy tdy, int nx, int ny, int nz, const double lower[3], const double upper[3]);
 TDyErrorCode TDySetExtrudedMesh(TDy tdy, int nv2, const double *xy, int nc2, int nvpc, const int *cells2d,
                                 int nlayers, const double *z);
+/* Extension: a batch of independent extruded meshes (instances) in one
+ * handle, for batched evaluation and solves.  Block b has nv2[b] surface
+ * vertices, nc2[b] polygons of nvpc vertices and nlayers[b] layers; xy,
+ * cells2d (indices local to the block) and z hold the blocks one after the
+ * other in the layout of TDySetExtrudedMesh.  Cells, vertices, faces and
+ * boundary faces are numbered block by block, so instance b owns a contiguous
+ * cell range; no face joins two blocks. */
+TDyErrorCode TDySetExtrudedMeshes(TDy tdy, int nblocks, const int *nv2, const double *xy, const int *nc2, int nvpc,
+                                  const int *cells2d, const int *nlayers, const double *z);
 
 /* Material properties: include/tdycore.h:150-171. */
 TDyErrorCode TDySetWaterDensityType(TDy tdy, TDyWaterDensityType type);
@@ -195,6 +204,41 @@ TDyErrorCode TDyMPFAOIFunction(TDy tdy, double t, const double *U, const double 
 TDyErrorCode TDyMPFAOIJacobian(TDy tdy, double t, const double *U, const double *U_t, double shift, double *J);
 TDyErrorCode TDyMPFAOIFunctionIJacobian(TDy tdy, double t, const double *U, const double *U_t, double shift,
                                         double *R, double *J);
+/* ---------------------------------------------------------------------- */
+/* Extension: device-resident backward-Euler Newton solve (no reference
+ * counterpart: the reference hands F and J to PETSc's SNES and KSP).  One
+ * call advances every instance of the handle (each block of
+ * TDySetExtrudedMeshes, or the single mesh) by dt: presolve at dU, then Newton
+ * with the FP64 residual until ||F|| <= rtol ||F_0|| (or <= atol) per
+ * instance (or until the Newton step is below stol ||U||, PETSc's step test),
+ * with a backtracking line search per instance; each Newton system solved by BiCGStab preconditioned with exact
+ * solves of the vertical lines of the extruded blocks, in FP32 (the Jacobian
+ * is rounded to FP32) or FP64.  dU (device, ncells) holds U_n on entry and
+ * U_{n+1} on return. */
+typedef struct {
+  double rtol;         /* relative FP64 residual per instance (default 1e-8) */
+  double atol;         /* absolute residual (default 0) */
+  int max_it;          /* Newton iterations (default 50, as PETSc SNES) */
+  int linear_fp32;     /* 1: FP32 Jacobian and inner solve (default); 0: FP64 */
+  double linear_rtol;  /* BiCGStab relative tolerance per instance (default 1e-6) */
+  int linear_max_it;   /* BiCGStab iterations per Newton iteration (default 400) */
+  double stol;         /* step tolerance: converged when ||step|| < stol ||U|| per instance
+                          (PETSc's CONVERGED_SNORM_RELATIVE; default 1e-8) */
+} TDyNewtonOptions;
+typedef struct {
+  int newton_iterations;        /* largest over the instances */
+  long long linear_iterations;  /* BiCGStab iterations, summed over instances and Newton iterations */
+  int converged;                /* instances that met the tolerance */
+  int ninstances;
+  double max_rel_residual;      /* largest final ||F|| / ||F_0|| */
+} TDyNewtonStats;
+TDyErrorCode TDyNewtonOptionsDefault(TDyNewtonOptions *o);
+TDyErrorCode TDyGetNumInstances(TDy tdy, int *n);
+/* inst_iterations and inst_rel_residual (host, ninstances entries) may be NULL. */
+TDyErrorCode TDyBackwardEulerStepDevice(TDy tdy, double dt, double *dU, const TDyNewtonOptions *opt,
+                                        TDyNewtonStats *stats, int *inst_iterations, double *inst_rel_residual,
+                                        void *stream);
+
 /* ---------------------------------------------------------------------- */
 /* TS variants with the same flux kernels (TDySetDiscretization MPFA_O_TRANSIENTVAR
  * or MPFA_O_DAE; src/tdycore.c:1902-1908). */

@@ -65,6 +65,16 @@ class TDyMPFAOSetupView(ctypes.Structure):
     ]
 
 
+class NewtonOptions(ctypes.Structure):
+    _fields_ = [("rtol", c_double), ("atol", c_double), ("max_it", c_int), ("linear_fp32", c_int),
+                ("linear_rtol", c_double), ("linear_max_it", c_int), ("stol", c_double)]
+
+
+class NewtonStats(ctypes.Structure):
+    _fields_ = [("newton_iterations", c_int), ("linear_iterations", c_longlong), ("converged", c_int),
+                ("ninstances", c_int), ("max_rel_residual", c_double)]
+
+
 def _sig(name, *args):
     f = getattr(lib, name)
     f.argtypes = list(args)
@@ -82,6 +92,10 @@ _sig("TDyOptionsGetInt", c_char_p, _ip, _ip)
 _sig("TDyOptionsGetString", c_char_p, c_char_p, c_int, _ip)
 _sig("TDyOptionsHasName", c_char_p, _ip)
 _sig("TDyOutputRegression", c_void_p, _dp)
+_sig("TDyNewtonOptionsDefault", POINTER(NewtonOptions))
+_sig("TDyGetNumInstances", c_void_p, _ip)
+_sig("TDyBackwardEulerStepDevice", c_void_p, c_double, c_void_p, POINTER(NewtonOptions), POINTER(NewtonStats), _ip,
+     _dp, c_void_p)
 _sig("TDyCreate", c_void_p, POINTER(c_void_p))
 _sig("TDyDestroy", POINTER(c_void_p))
 _sig("TDySetMode", c_void_p, c_int)
@@ -92,6 +106,7 @@ _sig("TDySetup", c_void_p)
 _sig("TDySetupHost", c_void_p)
 _sig("TDySetBoxMesh", c_void_p, c_int, c_int, c_int, _dp, _dp)
 _sig("TDySetExtrudedMesh", c_void_p, c_int, _dp, c_int, c_int, _ip, c_int, _dp)
+_sig("TDySetExtrudedMeshes", c_void_p, c_int, _ip, _dp, _ip, c_int, _ip, _ip, _dp)
 _sig("TDySetWaterDensityType", c_void_p, c_int)
 _sig("TDySetWaterViscosityType", c_void_p, c_int)
 _sig("TDySetConstantPorosity", c_void_p, c_double)
@@ -217,6 +232,22 @@ def options_has_name(name: str) -> bool:
     return bool(f.value)
 
 
+def _eval_points(f, n, x, out, dtype):
+    """Evaluates f(x, y, z) at n points (x: 3n doubles) into out: once on
+    numpy arrays when f accepts them, else point by point."""
+    pts = np.ctypeslib.as_array(x, shape=(3 * n,)).reshape(n, 3)
+    res = np.ctypeslib.as_array(out, shape=(n,))
+    try:
+        v = np.asarray(f(pts[:, 0], pts[:, 1], pts[:, 2]))
+        if v.shape in ((), (n,)):
+            res[:] = np.broadcast_to(v, (n,)).astype(dtype)
+            return
+    except (TypeError, ValueError):
+        pass
+    for i in range(n):
+        res[i] = dtype(f(*pts[i]))
+
+
 class TDy:
     """One MPFA-O Richards instance; owns its device buffers."""
 
@@ -282,6 +313,27 @@ class TDy:
         z = _f64(z).reshape(-1, xy.shape[0])
         check(lib.TDySetExtrudedMesh(self._h, xy.shape[0], _as_dp(xy), cells2d.shape[0], nvpc,
                                      cells2d.ctypes.data_as(_ip), z.shape[0] - 1, _as_dp(z)), "TDySetExtrudedMesh")
+        return self
+
+    def set_extruded_meshes(self, blocks):
+        """A batch of independent extruded meshes: ``blocks`` is a list of
+        (xy, cells2d, z) as for set_extruded_mesh (same polygon size)."""
+        nvpc = {np.asarray(c).shape[1] for _, c, _ in blocks}
+        if len(nvpc) != 1:
+            raise ValueError("all blocks must use the same polygon size")
+        nvpc = nvpc.pop()
+        xys = [_f64(xy).reshape(-1, 2) for xy, _, _ in blocks]
+        nv2 = _i32([a.shape[0] for a in xys])
+        nc2 = _i32([np.asarray(c).shape[0] for _, c, _ in blocks])
+        zs = [_f64(z).reshape(-1, a.shape[0]) for (_, _, z), a in zip(blocks, xys)]
+        nl = _i32([z.shape[0] - 1 for z in zs])
+        xy = _f64(np.concatenate([a.ravel() for a in xys]))
+        c2 = _i32(np.concatenate([np.asarray(c, dtype=np.int32).ravel() for _, c, _ in blocks]))
+        z = _f64(np.concatenate([a.ravel() for a in zs]))
+        check(lib.TDySetExtrudedMeshes(self._h, len(blocks), nv2.ctypes.data_as(_ip), _as_dp(xy),
+                                       nc2.ctypes.data_as(_ip), nvpc, c2.ctypes.data_as(_ip), nl.ctypes.data_as(_ip),
+                                       _as_dp(z)), "TDySetExtrudedMeshes")
+        self.block_cells = np.concatenate([[0], np.cumsum(nc2.astype(np.int64) * nl)])
         return self
 
     # materials --------------------------------------------------------------
@@ -387,8 +439,7 @@ class TDy:
         """f(x, y, z) -> pressure, evaluated once per boundary face centroid."""
 
         def wrapped(n, x, out):
-            for i in range(n):
-                out[i] = f(x[3 * i], x[3 * i + 1], x[3 * i + 2])
+            _eval_points(f, n, x, out, np.float64)
 
         cb = ScalarSpatialFunction(wrapped)
         self._keep.append(cb)
@@ -399,8 +450,7 @@ class TDy:
         """f(x, y, z) -> DIRICHLET_BC | NEUMANN_BC | SEEPAGE_BC per boundary face."""
 
         def wrapped(n, x, out):
-            for i in range(n):
-                out[i] = int(f(x[3 * i], x[3 * i + 1], x[3 * i + 2]))
+            _eval_points(f, n, x, out, np.int32)
 
         cb = IntegerSpatialFunction(wrapped)
         self._keep.append(cb)
@@ -549,6 +599,32 @@ class TDy:
         R = np.empty(2 * self.ncells)
         check(lib.TDyMPFAOIFunctionDAE(self._h, t, _as_dp(u), _as_dp(ut), _as_dp(R)), "TDyMPFAOIFunctionDAE")
         return R
+
+    # device Newton -------------------------------------------------------------
+    def num_instances(self) -> int:
+        n = c_int()
+        check(lib.TDyGetNumInstances(self._h, byref(n)), "TDyGetNumInstances")
+        return n.value
+
+    def backward_euler_step_device(self, dU, dt, rtol=1e-8, atol=0.0, max_it=50, fp32=True, linear_rtol=1e-6,
+                                   linear_max_it=400, stol=1e-8, stream=None):
+        """One backward-Euler step of every instance with the device Newton
+        solver; dU (device float64 tensor, ncells) holds U_n and receives
+        U_{n+1}.  Returns (stats dict, per-instance Newton iterations,
+        per-instance final ||F||/||F_0||)."""
+        o = NewtonOptions()
+        check(lib.TDyNewtonOptionsDefault(byref(o)), "TDyNewtonOptionsDefault")
+        o.rtol, o.atol, o.max_it, o.linear_fp32 = rtol, atol, max_it, int(bool(fp32))
+        o.linear_rtol, o.linear_max_it, o.stol = linear_rtol, linear_max_it, stol
+        st = NewtonStats()
+        ni = self.num_instances()
+        its = np.zeros(ni, dtype=np.int32)
+        rel = np.zeros(ni)
+        check(lib.TDyBackwardEulerStepDevice(self._h, dt, self._ptr(dU), byref(o), byref(st),
+                                             its.ctypes.data_as(_ip), _as_dp(rel), self._ptr(stream)),
+              "TDyBackwardEulerStepDevice")
+        stats = {k: getattr(st, k) for k, _ in NewtonStats._fields_}
+        return stats, its, rel
 
     # device-pointer forms (torch tensors or raw pointers) -------------------
     @staticmethod

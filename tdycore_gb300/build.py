@@ -24,7 +24,7 @@ ORACLE_LIB = ORACLE_DIR / "_build" / "libmpfao_oracle.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O3", "--expt-relaxed-constexpr"]
-SOURCES = ["tdy_mesh.cpp", "tdy_setup.cpp", "tdy_api.cpp", "tdy_kernels.cu", "tdy_setup_kernels.cu"]
+SOURCES = ["tdy_mesh.cpp", "tdy_setup.cpp", "tdy_api.cpp", "tdy_kernels.cu", "tdy_setup_kernels.cu", "tdy_solver.cu"]
 
 
 def _nvcc() -> str:

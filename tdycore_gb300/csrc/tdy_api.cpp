@@ -346,7 +346,7 @@ TDyErrorCode TDySetExtrudedMesh(TDy tdy, int nv2, const double *xy, int nc2, int
   if (!xy || !cells2d || !z) return set_error(TDY_ERR_ARG_NULL, "TDySetExtrudedMesh: null array");
   if (nv2 <= 0 || nc2 <= 0 || nlayers <= 0) return set_error(TDY_ERR_ARG_OUTOFRANGE, "TDySetExtrudedMesh: empty mesh");
   if (nvpc != 3 && nvpc != 4) return set_error(TDY_ERR_SUP, "TDySetExtrudedMesh: polygons must have 3 or 4 vertices");
-  ExtrudedInput &in = tdy->mesh_in;
+  ExtrudedInput in;
   in.set = true;
   in.nv2 = nv2;
   in.nc2 = nc2;
@@ -355,6 +355,38 @@ TDyErrorCode TDySetExtrudedMesh(TDy tdy, int nv2, const double *xy, int nc2, int
   in.xy.assign(xy, xy + 2 * (size_t)nv2);
   in.cells2d.assign(cells2d, cells2d + (size_t)nvpc * nc2);
   in.z.assign(z, z + (size_t)(nlayers + 1) * nv2);
+  tdy->mesh_blocks.assign(1, std::move(in));
+  return 0;
+}
+
+TDyErrorCode TDySetExtrudedMeshes(TDy tdy, int nblocks, const int *nv2, const double *xy, const int *nc2, int nvpc,
+                                  const int *cells2d, const int *nlayers, const double *z) {
+  TDY_CHECK_HANDLE(tdy);
+  TDY_CHECK_NOT_SETUP(tdy);
+  if (nblocks <= 0) return set_error(TDY_ERR_ARG_OUTOFRANGE, "TDySetExtrudedMeshes: no blocks");
+  if (!nv2 || !xy || !nc2 || !cells2d || !nlayers || !z) return set_error(TDY_ERR_ARG_NULL, "TDySetExtrudedMeshes: null array");
+  if (nvpc != 3 && nvpc != 4) return set_error(TDY_ERR_SUP, "TDySetExtrudedMeshes: polygons must have 3 or 4 vertices");
+  std::vector<ExtrudedInput> blocks(nblocks);
+  size_t oxy = 0, oc = 0, oz = 0;
+  for (int b = 0; b < nblocks; b++) {
+    if (nv2[b] <= 0 || nc2[b] <= 0 || nlayers[b] <= 0)
+      return set_error(TDY_ERR_ARG_OUTOFRANGE, "TDySetExtrudedMeshes: block %d is empty", b);
+    ExtrudedInput &in = blocks[b];
+    in.set = true;
+    in.nv2 = nv2[b];
+    in.nc2 = nc2[b];
+    in.nvpc = nvpc;
+    in.nlayers = nlayers[b];
+    in.xy.assign(xy + oxy, xy + oxy + 2 * (size_t)nv2[b]);
+    in.cells2d.assign(cells2d + oc, cells2d + oc + (size_t)nvpc * nc2[b]);
+    in.z.assign(z + oz, z + oz + (size_t)(nlayers[b] + 1) * nv2[b]);
+    for (int k : in.cells2d)
+      if (k < 0 || k >= nv2[b]) return set_error(TDY_ERR_ARG_OUTOFRANGE, "TDySetExtrudedMeshes: block %d vertex index %d", b, k);
+    oxy += 2 * (size_t)nv2[b];
+    oc += (size_t)nvpc * nc2[b];
+    oz += (size_t)(nlayers[b] + 1) * nv2[b];
+  }
+  tdy->mesh_blocks = std::move(blocks);
   return 0;
 }
 
@@ -702,18 +734,20 @@ static int build_boundary(TDy t) {
   b.value.assign(m.nb, 0.0);
   b.rho.assign(m.nb, 0.0);
   b.vis.assign(m.nb, 0.0);
+  // the spatial functions take n points at once: one call for all faces
+  std::vector<double> xs(3 * (size_t)m.nb);
+  for (int i = 0; i < m.nb; i++)
+    for (int d = 0; d < 3; d++) xs[3 * (size_t)i + d] = m.face_cen[3 * (size_t)m.bnd_face[i] + d];
+  if (t->bc_type_func && m.nb > 0) {
+    t->bc_type_func(m.nb, xs.data(), b.type.data());
+    for (int i = 0; i < m.nb; i++)
+      if (b.type[i] < DIRICHLET_BC || b.type[i] > SEEPAGE_BC)
+        return set_error(TDY_ERR_ARG_OUTOFRANGE, "bad boundary type %d", b.type[i]);
+  }
+  if (t->bc_pressure_func && m.nb > 0) t->bc_pressure_func(m.nb, xs.data(), b.value.data());
   for (int i = 0; i < m.nb; i++) {
-    int f = m.bnd_face[i];
-    double x[3] = {m.face_cen[3 * (size_t)f], m.face_cen[3 * (size_t)f + 1], m.face_cen[3 * (size_t)f + 2]};
-    if (t->bc_type_func) {
-      int ty = t->opt.bc_type;
-      t->bc_type_func(1, x, &ty);
-      if (ty < DIRICHLET_BC || ty > SEEPAGE_BC) return set_error(TDY_ERR_ARG_OUTOFRANGE, "bad boundary type %d", ty);
-      b.type[i] = ty;
-    }
     if (t->bc_pressure_func) {
       b.has_value[i] = 1;
-      t->bc_pressure_func(1, x, &b.value[i]);
     } else if (t->opt.has_pressure_bc_value) {
       b.has_value[i] = 1;
       b.value[i] = t->opt.pressure_bc_value;
@@ -729,12 +763,20 @@ static int setup_host(TDy tdy) {
   if (!(tdy->flags & TDY_FLAG_DISC)) return set_error(TDY_ERR_USER, "You must call TDySetDiscretization before TDySetup()");
   if (!(tdy->flags & TDY_FLAG_OPTIONS)) return set_error(TDY_ERR_USER, "You must call TDySetFromOptions before TDySetup()");
   if (tdy->is_setup) return set_error(TDY_ERR_USER, "TDySetup called twice");
-  if (!tdy->mesh_in.set) return set_error(TDY_ERR_USER, "no mesh: call TDySetBoxMesh or TDySetExtrudedMesh before TDySetup");
+  if (tdy->mesh_blocks.empty())
+    return set_error(TDY_ERR_USER, "no mesh: call TDySetBoxMesh, TDySetExtrudedMesh or TDySetExtrudedMeshes before TDySetup");
   // TDyRegressionInitialize (src/tdyregression.c:38-45)
   if (tdy->opt.regression_testing && tdy->opt.regression_filename.empty())
     return set_error(TDY_ERR_USER, "Need to specify a regression filename via -tdy_regression_test_filename");
   int ierr;
-  if ((ierr = build_extruded_mesh(tdy->mesh_in, tdy->mesh))) return ierr;
+  if (tdy->mesh_blocks.size() == 1) {
+    if ((ierr = build_extruded_mesh(tdy->mesh_blocks[0], tdy->mesh))) return ierr;
+  } else {
+    std::vector<Mesh> parts(tdy->mesh_blocks.size());
+    for (size_t b = 0; b < parts.size(); b++)
+      if ((ierr = build_extruded_mesh(tdy->mesh_blocks[b], parts[b]))) return ierr;
+    merge_meshes(parts, tdy->mesh);
+  }
   if ((ierr = build_materials(tdy))) return ierr;
   if ((ierr = build_boundary(tdy))) return ierr;
   if ((ierr = mpfao_setup(tdy->opt, tdy->mesh, tdy->mat, tdy->bnd, tdy->setup))) return ierr;
@@ -763,6 +805,7 @@ TDyErrorCode TDySetupHost(TDy tdy) {
 
 TDyErrorCode TDyDestroy(TDy *tdy) {
   if (!tdy || !*tdy) return 0;
+  device_solver_destroy(*tdy);
   device_destroy(*tdy);
   delete *tdy;
   *tdy = nullptr;
@@ -961,6 +1004,38 @@ TDyErrorCode TDyMPFAOIJacobian(TDy tdy, double t, const double *U, const double 
   if (!U || !U_t || !J) return set_error(TDY_ERR_ARG_NULL, "null array");
   return device_eval_host(tdy, FORM_TS, t, U, U_t, shift, nullptr, J);
 }
+TDyErrorCode TDyNewtonOptionsDefault(TDyNewtonOptions *o) {
+  if (!o) return set_error(TDY_ERR_ARG_NULL, "TDyNewtonOptionsDefault: null");
+  o->rtol = 1e-8;
+  o->atol = 0.0;
+  o->max_it = 50;
+  o->linear_fp32 = 1;
+  o->linear_rtol = 1e-6;
+  o->linear_max_it = 400;
+  o->stol = 1e-8;
+  return 0;
+}
+TDyErrorCode TDyGetNumInstances(TDy tdy, int *n) {
+  TDY_CHECK_HANDLE(tdy);
+  if (!n) return set_error(TDY_ERR_ARG_NULL, "TDyGetNumInstances: null");
+  *n = (int)tdy->mesh_blocks.size();
+  return 0;
+}
+TDyErrorCode TDyBackwardEulerStepDevice(TDy tdy, double dt, double *dU, const TDyNewtonOptions *opt,
+                                        TDyNewtonStats *stats, int *inst_iterations, double *inst_rel_residual,
+                                        void *stream) {
+  TDY_CHECK_HANDLE(tdy);
+  TDY_CHECK_DEVICE(tdy);
+  if (!dU) return set_error(TDY_ERR_ARG_NULL, "TDyBackwardEulerStepDevice: null dU");
+  if (!(dt > 0.0)) return set_error(TDY_ERR_ARG_OUTOFRANGE, "TDyBackwardEulerStepDevice: dt must be > 0");
+  TDyNewtonOptions o;
+  TDyNewtonOptionsDefault(&o);
+  if (opt) o = *opt;
+  if (o.max_it < 0 || o.linear_max_it < 1 || !(o.rtol >= 0.0) || !(o.linear_rtol > 0.0))
+    return set_error(TDY_ERR_ARG_OUTOFRANGE, "TDyBackwardEulerStepDevice: invalid options");
+  return device_be_solve(tdy, dt, dU, o, stats, inst_iterations, inst_rel_residual, stream);
+}
+
 TDyErrorCode TDyMPFAOTransientVariable(TDy tdy, const double *U, double *C) {
   TDY_CHECK_HANDLE(tdy);
   TDY_CHECK_DEVICE(tdy);

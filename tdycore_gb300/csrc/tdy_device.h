@@ -30,6 +30,12 @@ int device_eval_noalloc(_p_TDy *t, const double *dU, double *dR, double *dJ, voi
 int device_transient_variable_host(_p_TDy *t, const double *U, double *C, double *dC);
 // DAE form: U, U_t, R interleaved [P, M] per cell (2 * ncells values).
 int device_eval_dae_host(_p_TDy *t, double time, const double *U2, const double *Ut2, double *R2);
+void *device_default_stream(_p_TDy *t);
+// Backward-Euler Newton solve of every instance (tdy_solver.cu).
+int device_be_solve(_p_TDy *t, double dt, double *dU, const TDyNewtonOptions &o, TDyNewtonStats *stats,
+                    int *inst_its, double *inst_rel, void *stream);
+void device_solver_destroy(_p_TDy *t);
+int device_num_instances(_p_TDy *t);
 // Trans of the canonical vertices into d_Tc (-tdy_mpfao_setup_on_device).
 int device_canon_trans(const _p_TDy *t, const int *d_cellc, const int *d_facec, double *d_Tc);
 

@@ -98,6 +98,9 @@ struct Mesh {
 
 // Builds the z-extruded mesh: connectivity, geometry and face orientation.
 int build_extruded_mesh(const ExtrudedInput &in, Mesh &m);
+// Disjoint union of block meshes: vertices, cells, faces and boundary faces
+// numbered block by block (block b's entities follow those of blocks < b).
+void merge_meshes(const std::vector<Mesh> &parts, Mesh &m);
 
 // ---------------------------------------------------------------------------
 // Cell material and characteristic-curve parameters (SoA).
@@ -196,6 +199,7 @@ void eos_viscosity(int type, double p, double *vis, double *dvis, double *d2vis)
 int mualem_smoothing_coeffs(double m, double x0, double x1, double x2, double dx, double coeffs[4]);
 
 struct DeviceState;  // defined in the CUDA translation unit
+struct SolverState;  // tdy_solver.cu
 
 }  // namespace tdy
 
@@ -206,7 +210,9 @@ struct _p_TDy {
   int mode = RICHARDS;
   int discretization = MPFA_O;
   tdy::Options opt;
-  tdy::ExtrudedInput mesh_in;
+  // one extruded block (TDySetBoxMesh, TDySetExtrudedMesh) or several
+  // independent ones (TDySetExtrudedMeshes: a batch of instances)
+  std::vector<tdy::ExtrudedInput> mesh_blocks;
   tdy::ScalarSpec porosity, sr;
   tdy::PermSpec perm;
   std::vector<std::pair<int, std::vector<double>>> vg_over, gardner_over;
@@ -225,6 +231,7 @@ struct _p_TDy {
   bool have_prev = false;
   std::vector<double> U_prev;
   tdy::DeviceState *dev = nullptr;
+  tdy::SolverState *solver = nullptr;  // device Newton solver, on first use
 };
 
 enum : unsigned {

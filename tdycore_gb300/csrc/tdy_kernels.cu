@@ -1043,6 +1043,8 @@ int device_eval(_p_TDy *t, int form, double time, const double *dU, const double
   return 0;
 }
 
+void *device_default_stream(_p_TDy *t) { return t->dev ? (void *)t->dev->stream : nullptr; }
+
 int device_set_timers(_p_TDy *t, int on) {
   DeviceState *d = t->dev;
   if (on && !d->ev[0])

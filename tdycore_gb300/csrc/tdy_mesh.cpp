@@ -300,4 +300,48 @@ int build_extruded_mesh(const ExtrudedInput &in, Mesh &m) {
   return 0;
 }
 
+void merge_meshes(const std::vector<Mesh> &parts, Mesh &m) {
+  m = Mesh();
+  m.cell_vert_off.push_back(0);
+  m.cell_face_off.push_back(0);
+  m.face_vert_off.push_back(0);
+  m.vert_cell_off.push_back(0);
+  m.vert_face_off.push_back(0);
+  for (const Mesh &p : parts) {
+    const int v0 = m.nv, c0 = m.nc, f0 = m.nf, b0 = m.nb;
+    auto append = [](std::vector<int> &dst, const std::vector<int> &src, int add) {
+      for (int x : src) dst.push_back(x + add);
+    };
+    auto append_off = [](std::vector<int> &dst, const std::vector<int> &src) {
+      const int base = dst.back();
+      for (size_t i = 1; i < src.size(); i++) dst.push_back(src[i] + base);
+    };
+    m.vx.insert(m.vx.end(), p.vx.begin(), p.vx.end());
+    append_off(m.cell_vert_off, p.cell_vert_off);
+    append(m.cell_verts, p.cell_verts, v0);
+    append_off(m.cell_face_off, p.cell_face_off);
+    append(m.cell_faces, p.cell_faces, f0);
+    m.cell_cen.insert(m.cell_cen.end(), p.cell_cen.begin(), p.cell_cen.end());
+    m.cell_vol.insert(m.cell_vol.end(), p.cell_vol.begin(), p.cell_vol.end());
+    append_off(m.face_vert_off, p.face_vert_off);
+    append(m.face_verts, p.face_verts, v0);
+    // reference encoding: cell id, or -(boundary index + 1)
+    for (int x : p.face_cell0) m.face_cell0.push_back(x >= 0 ? x + c0 : x - b0);
+    for (int x : p.face_cell1) m.face_cell1.push_back(x >= 0 ? x + c0 : x - b0);
+    m.face_cen.insert(m.face_cen.end(), p.face_cen.begin(), p.face_cen.end());
+    m.face_nrm.insert(m.face_nrm.end(), p.face_nrm.begin(), p.face_nrm.end());
+    m.face_area.insert(m.face_area.end(), p.face_area.begin(), p.face_area.end());
+    for (int x : p.face_bnd) m.face_bnd.push_back(x >= 0 ? x + b0 : x);
+    append(m.bnd_face, p.bnd_face, f0);
+    append_off(m.vert_cell_off, p.vert_cell_off);
+    append(m.vert_cells, p.vert_cells, c0);
+    append_off(m.vert_face_off, p.vert_face_off);
+    append(m.vert_faces, p.vert_faces, f0);
+    m.nv += p.nv;
+    m.nc += p.nc;
+    m.nf += p.nf;
+    m.nb += p.nb;
+  }
+}
+
 }  // namespace tdy

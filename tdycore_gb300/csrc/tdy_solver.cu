@@ -1,0 +1,676 @@
+// tdy_solver.cu -- device-resident backward-Euler Newton solve of one or many
+// independent instances (the blocks of TDySetExtrudedMeshes) in one handle.
+//
+// Each Newton iteration evaluates the FP64 residual and the Jacobian with the
+// handle's kernels for every instance at once, takes per-instance residual
+// norms (the only values the host reads), and solves J y = F with
+// right-preconditioned BiCGStab:
+//   * Krylov vectors and the Jacobian copy in FP32 (default) or FP64; the
+//     residual, the Newton update x -= y and the convergence test stay FP64;
+//   * every instance keeps its own BiCGStab scalars and stops on its own
+//     tolerance (device-side masks, no host round trip per iteration);
+//   * preconditioner: exact solves of the vertical lines (the tridiagonal
+//     coupling of each column of an extruded block, Thomas algorithm, one
+//     thread per column), which carries the stiff vertical coupling of thin
+//     layers;
+//   * one BiCGStab iteration is captured once as a CUDA graph and replayed;
+//   * the sparse matrix-vector product's threads per row (1, 4 or 8) are
+//     picked by timing the candidates on the first solve.
+// No reference counterpart: the reference hands F and J to PETSc's SNES/KSP.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "tdy_device.h"
+
+namespace tdy {
+
+namespace {
+
+#define SCUDA(call)                                                                             \
+  do {                                                                                          \
+    cudaError_t e_ = (call);                                                                    \
+    if (e_ != cudaSuccess)                                                                      \
+      return set_error(TDY_ERR_GPU, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+  } while (0)
+
+inline unsigned nblk(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+// per-instance scalars, [slot][nseg]
+enum { S_RHO = 0, S_ALPHA, S_OMEGA, S_BETA, S_BNORM2, S_T1, S_T2, S_HALF, S_NSCAL };
+
+struct Krylov {
+  bool ready = false;
+  void *Jv = nullptr;                                  // matrix values (T)
+  void *b = nullptr, *r = nullptr, *r0 = nullptr, *p = nullptr, *v = nullptr, *s = nullptr, *t = nullptr,
+       *ph = nullptr, *sh = nullptr, *y = nullptr;     // vectors (T)
+  void *la = nullptr, *lcp = nullptr, *linv = nullptr; // line factors (T)
+  cudaGraphExec_t graph = nullptr;
+  cudaStream_t graph_stream = nullptr;
+  int tpr = 0;  // spmv threads per row (autotuned)
+};
+
+}  // namespace
+
+struct SolverState {
+  int n = 0, nnz = 0, nseg = 0, nlines = 0;
+  std::vector<int> h_seg_off;
+  int *rowptr = nullptr, *colidx = nullptr, *seg_off = nullptr, *cell_seg = nullptr;
+  int *line_off = nullptr, *line_cells = nullptr, *pos_d = nullptr, *pos_lo = nullptr, *pos_hi = nullptr;
+  double *x = nullptr, *xb = nullptr, *F = nullptr, *J = nullptr, *fn2 = nullptr, *scal = nullptr, *lam = nullptr;
+  int *trial = nullptr, *commit = nullptr;
+  int *newt_active = nullptr, *lin_active = nullptr, *lin_its = nullptr;
+  double linear_rtol = -1.0;
+  Krylov k32, k64;
+  std::vector<void *> allocs;
+  ~SolverState() {
+    for (Krylov *k : {&k32, &k64})
+      if (k->graph) cudaGraphExecDestroy(k->graph);
+    for (void *p : allocs) cudaFree(p);
+  }
+};
+
+namespace {
+
+template <class T>
+int salloc(SolverState *s, T **p, size_t n) {
+  cudaError_t e = cudaMalloc((void **)p, std::max<size_t>(n, 1) * sizeof(T));
+  if (e != cudaSuccess) return set_error(TDY_ERR_GPU, "cudaMalloc: %s", cudaGetErrorString(e));
+  s->allocs.push_back(*p);
+  return 0;
+}
+template <class T>
+int sup(SolverState *s, T **p, const std::vector<T> &h) {
+  int ierr = salloc(s, p, h.size());
+  if (ierr) return ierr;
+  cudaError_t e = cudaMemcpy(*p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return set_error(TDY_ERR_GPU, "cudaMemcpy: %s", cudaGetErrorString(e));
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// kernels
+
+template <class T>
+__global__ void cast_kernel(long long n, const double *a, T *b) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (T)a[i];
+}
+
+// out[s] = sum over instance s of a*b (and out2[s] of c*d), FP64 accumulation;
+// one block per instance
+template <class TA, class TB>
+__global__ void __launch_bounds__(256) seg_dot_kernel(const int *seg_off, const TA *a, const TB *b, const TA *c,
+                                                      const TB *d, double *out, double *out2) {
+  __shared__ double sh[2][256];
+  const int s = blockIdx.x;
+  const int i0 = seg_off[s], i1 = seg_off[s + 1];
+  double acc = 0.0, acc2 = 0.0;
+  for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+    acc += (double)a[i] * (double)b[i];
+    if (c) acc2 += (double)c[i] * (double)d[i];
+  }
+  sh[0][threadIdx.x] = acc;
+  sh[1][threadIdx.x] = acc2;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) {
+      sh[0][threadIdx.x] += sh[0][threadIdx.x + w];
+      sh[1][threadIdx.x] += sh[1][threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out[s] = sh[0][0];
+    if (c) out2[s] = sh[1][0];
+  }
+}
+
+// y = A x over the CSR pattern with TPR threads per row
+template <class T, int TPR>
+__global__ void __launch_bounds__(256) spmv_kernel(int n, const int *rowptr, const int *colidx, const T *A, const T *x,
+                                                   T *y) {
+  const long long gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int row = (int)(gt / TPR), lane = (int)(gt % TPR);
+  T acc = 0;
+  if (row < n)
+    for (int k = rowptr[row] + lane; k < rowptr[row + 1]; k += TPR) acc += A[k] * x[colidx[k]];
+#pragma unroll
+  for (int o = TPR / 2; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o, TPR);
+  if (row < n && lane == 0) y[row] = acc;
+}
+
+// Thomas factorisation of every vertical line from the FP64 Jacobian
+template <class T>
+__global__ void line_factor_kernel(int nlines, const int *line_off, const int *pd, const int *plo, const int *phi,
+                                   const double *J, T *la, T *lcp, T *linv) {
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= nlines) return;
+  double cp = 0.0;
+  for (int k = line_off[l]; k < line_off[l + 1]; k++) {
+    const double b = J[pd[k]], a = plo[k] >= 0 ? J[plo[k]] : 0.0, c = phi[k] >= 0 ? J[phi[k]] : 0.0;
+    double den = b - a * cp;
+    if (den == 0.0) den = (b != 0.0) ? b : 1.0;  // singular line: fall back to its diagonal
+    const double inv = 1.0 / den;
+    cp = c * inv;
+    la[k] = (T)a;
+    lcp[k] = (T)cp;
+    linv[k] = (T)inv;
+  }
+}
+
+// out = (line-tridiagonal)^-1 in
+template <class T>
+__global__ void line_solve_kernel(int nlines, const int *line_off, const int *line_cells, const T *la, const T *lcp,
+                                  const T *linv, const T *in, T *out) {
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= nlines) return;
+  const int k0 = line_off[l], k1 = line_off[l + 1];
+  T prev = 0;
+  for (int k = k0; k < k1; k++) {
+    const int i = line_cells[k];
+    prev = (in[i] - la[k] * prev) * linv[k];
+    out[i] = prev;
+  }
+  T next = 0;
+  for (int k = k1 - 1; k >= k0; k--) {
+    const int i = line_cells[k];
+    next = out[i] - lcp[k] * next;
+    out[i] = next;
+  }
+}
+
+template <class T>
+__global__ void init_kernel(int n, const int *cell_seg, const int *active, const double *F, T *b, T *r, T *r0, T *p,
+                            T *v, T *y) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const T f = active[cell_seg[i]] ? (T)F[i] : (T)0;
+  b[i] = f;
+  r[i] = f;
+  r0[i] = f;
+  p[i] = 0;
+  v[i] = 0;
+  y[i] = 0;
+}
+
+__global__ void init_scalars_kernel(int nseg, const int *newt_active, int *lin_active, int *lin_its, double *scal) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nseg) return;
+  scal[S_RHO * nseg + s] = 1.0;
+  scal[S_ALPHA * nseg + s] = 1.0;
+  scal[S_OMEGA * nseg + s] = 1.0;
+  scal[S_HALF * nseg + s] = 0.0;
+  lin_active[s] = newt_active[s] && scal[S_BNORM2 * nseg + s] > 0.0;
+}
+
+// after rho_new = (r0, r) in T1
+__global__ void scal_beta_kernel(int nseg, int *act, double *sc) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nseg || !act[s]) return;
+  const double rn = sc[S_T1 * nseg + s];
+  if (rn == 0.0) {
+    act[s] = 0;
+    return;
+  }
+  sc[S_BETA * nseg + s] = (rn / sc[S_RHO * nseg + s]) * (sc[S_ALPHA * nseg + s] / sc[S_OMEGA * nseg + s]);
+  sc[S_RHO * nseg + s] = rn;
+}
+// after (r0, v) in T1
+__global__ void scal_alpha_kernel(int nseg, int *act, double *sc) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nseg || !act[s]) return;
+  const double d = sc[S_T1 * nseg + s];
+  if (d == 0.0) {
+    act[s] = 0;
+    return;
+  }
+  sc[S_ALPHA * nseg + s] = sc[S_RHO * nseg + s] / d;
+}
+// after (s, s) in T1: converged already at the half step?
+__global__ void scal_half_kernel(int nseg, const int *act, double *sc, double tol2) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nseg || !act[s]) return;
+  sc[S_HALF * nseg + s] = (sc[S_T1 * nseg + s] <= tol2 * sc[S_BNORM2 * nseg + s]) ? 1.0 : 0.0;
+}
+// after (t, t) in T1 and (t, s) in T2
+__global__ void scal_omega_kernel(int nseg, const int *act, double *sc) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nseg || !act[s]) return;
+  const double tt = sc[S_T1 * nseg + s];
+  sc[S_OMEGA * nseg + s] = tt > 0.0 ? sc[S_T2 * nseg + s] / tt : 0.0;
+}
+// after (r, r) in T1
+__global__ void scal_check_kernel(int nseg, int *act, int *its, double *sc, double tol2) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nseg || !act[s]) return;
+  its[s] += 1;
+  if (sc[S_HALF * nseg + s] != 0.0 || sc[S_T1 * nseg + s] <= tol2 * sc[S_BNORM2 * nseg + s] ||
+      sc[S_OMEGA * nseg + s] == 0.0)
+    act[s] = 0;
+}
+
+template <class T>
+__global__ void p_update_kernel(int n, const int *cs, const int *act, const double *sc, int nseg, const T *r, const T *v,
+                                T *p) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int s = cs[i];
+  if (!act[s]) return;
+  const T beta = (T)sc[S_BETA * nseg + s], omega = (T)sc[S_OMEGA * nseg + s];
+  p[i] = r[i] + beta * (p[i] - omega * v[i]);
+}
+template <class T>
+__global__ void s_update_kernel(int n, const int *cs, const int *act, const double *sc, int nseg, const T *r, const T *v,
+                                T *sv) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int s = cs[i];
+  if (!act[s]) return;
+  sv[i] = r[i] - (T)sc[S_ALPHA * nseg + s] * v[i];
+}
+template <class T>
+__global__ void xr_update_kernel(int n, const int *cs, const int *act, const double *sc, int nseg, const T *ph,
+                                 const T *sh, const T *sv, const T *tv, T *y, T *r) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int s = cs[i];
+  if (!act[s]) return;
+  const T alpha = (T)sc[S_ALPHA * nseg + s];
+  if (sc[S_HALF * nseg + s] != 0.0) {
+    y[i] += alpha * ph[i];
+    return;
+  }
+  const T omega = (T)sc[S_OMEGA * nseg + s];
+  y[i] += alpha * ph[i] + omega * sh[i];
+  r[i] = sv[i] - omega * tv[i];
+}
+
+// trial point of the line search: x = xb - lam_s y for the instances on
+// trial, x = xb for the others (FP64 update)
+template <class T>
+__global__ void trial_kernel(int n, const int *cs, const int *trial, const double *lam, const T *y, const double *xb,
+                             double *x) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int s = cs[i];
+  x[i] = trial[s] ? xb[i] - lam[s] * (double)y[i] : xb[i];
+}
+// accepted trial points become the base
+__global__ void commit_kernel(int n, const int *cs, const int *commit, const double *x, double *xb) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (commit[cs[i]]) xb[i] = x[i];
+}
+
+// ---------------------------------------------------------------------------
+template <class T>
+int spmv(SolverState *s, const Krylov &k, const T *x, T *y, cudaStream_t st) {
+  const T *A = (const T *)k.Jv;
+  const long long threads = (long long)s->n * k.tpr;
+  switch (k.tpr) {
+    case 1:
+      spmv_kernel<T, 1><<<nblk(threads, 256), 256, 0, st>>>(s->n, s->rowptr, s->colidx, A, x, y);
+      break;
+    case 4:
+      spmv_kernel<T, 4><<<nblk(threads, 256), 256, 0, st>>>(s->n, s->rowptr, s->colidx, A, x, y);
+      break;
+    default:
+      spmv_kernel<T, 8><<<nblk(threads, 256), 256, 0, st>>>(s->n, s->rowptr, s->colidx, A, x, y);
+      break;
+  }
+  return 0;
+}
+
+template <class T>
+int dot(SolverState *s, const T *a, const T *b, const T *c, const T *d, int slot1, int slot2, cudaStream_t st) {
+  seg_dot_kernel<T, T><<<s->nseg, 256, 0, st>>>(s->seg_off, a, b, c, d, s->scal + (size_t)slot1 * s->nseg,
+                                                 c ? s->scal + (size_t)slot2 * s->nseg : nullptr);
+  return 0;
+}
+
+// one BiCGStab iteration for every active instance (the graph body)
+template <class T>
+void bicgstab_iteration(SolverState *s, Krylov &k, double tol2, cudaStream_t st) {
+  const int n = s->n, ns = s->nseg;
+  const unsigned gb = nblk(n, 256), sb = nblk(ns, 128), lb = nblk(s->nlines, 128);
+  T *r = (T *)k.r, *r0 = (T *)k.r0, *p = (T *)k.p, *v = (T *)k.v, *sv = (T *)k.s, *tv = (T *)k.t;
+  T *ph = (T *)k.ph, *sh = (T *)k.sh, *y = (T *)k.y;
+  const T *la = (const T *)k.la, *lcp = (const T *)k.lcp, *linv = (const T *)k.linv;
+  dot<T>(s, r0, r, nullptr, nullptr, S_T1, 0, st);
+  scal_beta_kernel<<<sb, 128, 0, st>>>(ns, s->lin_active, s->scal);
+  p_update_kernel<T><<<gb, 256, 0, st>>>(n, s->cell_seg, s->lin_active, s->scal, ns, r, v, p);
+  line_solve_kernel<T><<<lb, 128, 0, st>>>(s->nlines, s->line_off, s->line_cells, la, lcp, linv, p, ph);
+  spmv<T>(s, k, ph, v, st);
+  dot<T>(s, r0, v, nullptr, nullptr, S_T1, 0, st);
+  scal_alpha_kernel<<<sb, 128, 0, st>>>(ns, s->lin_active, s->scal);
+  s_update_kernel<T><<<gb, 256, 0, st>>>(n, s->cell_seg, s->lin_active, s->scal, ns, r, v, sv);
+  dot<T>(s, sv, sv, nullptr, nullptr, S_T1, 0, st);
+  scal_half_kernel<<<sb, 128, 0, st>>>(ns, s->lin_active, s->scal, tol2);
+  line_solve_kernel<T><<<lb, 128, 0, st>>>(s->nlines, s->line_off, s->line_cells, la, lcp, linv, sv, sh);
+  spmv<T>(s, k, sh, tv, st);
+  dot<T>(s, tv, tv, tv, sv, S_T1, S_T2, st);
+  scal_omega_kernel<<<sb, 128, 0, st>>>(ns, s->lin_active, s->scal);
+  xr_update_kernel<T><<<gb, 256, 0, st>>>(n, s->cell_seg, s->lin_active, s->scal, ns, ph, sh, sv, tv, y, r);
+  dot<T>(s, r, r, nullptr, nullptr, S_T1, 0, st);
+  scal_check_kernel<<<sb, 128, 0, st>>>(ns, s->lin_active, s->lin_its, s->scal, tol2);
+}
+
+template <class T>
+int krylov_alloc(SolverState *s, Krylov &k) {
+  if (k.ready) return 0;
+  int ierr;
+  T *p;
+  if ((ierr = salloc(s, &p, s->nnz))) return ierr;
+  k.Jv = p;
+  void **vecs[] = {&k.b, &k.r, &k.r0, &k.p, &k.v, &k.s, &k.t, &k.ph, &k.sh, &k.y, &k.la, &k.lcp, &k.linv};
+  for (void **vp : vecs) {
+    if ((ierr = salloc(s, &p, s->n))) return ierr;
+    *vp = p;
+  }
+  k.ready = true;
+  return 0;
+}
+
+// Picks the spmv threads per row by timing the candidates on the first solve
+// of the process; the choice is then kept for every handle, so an instance
+// gets the same bits alone and inside a batch (the threads per row set the
+// summation order).
+std::mutex g_tpr_mutex;
+int g_tpr[2] = {0, 0};  // float, double
+
+template <class T>
+int autotune_spmv(SolverState *s, Krylov &k, cudaStream_t st) {
+  if (k.tpr) return 0;
+  std::lock_guard<std::mutex> lk(g_tpr_mutex);
+  int &cached = g_tpr[sizeof(T) == sizeof(double) ? 1 : 0];
+  if (cached) {
+    k.tpr = cached;
+    return 0;
+  }
+  cudaEvent_t e0, e1;
+  SCUDA(cudaEventCreate(&e0));
+  SCUDA(cudaEventCreate(&e1));
+  float best = 1e30f;
+  int best_tpr = 1;
+  for (int tpr : {1, 4, 8}) {
+    k.tpr = tpr;
+    spmv<T>(s, k, (const T *)k.b, (T *)k.v, st);  // warm-up
+    cudaEventRecord(e0, st);
+    for (int it = 0; it < 5; it++) spmv<T>(s, k, (const T *)k.b, (T *)k.v, st);
+    cudaEventRecord(e1, st);
+    SCUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best) {
+      best = ms;
+      best_tpr = tpr;
+    }
+  }
+  k.tpr = best_tpr;
+  cached = best_tpr;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return 0;
+}
+
+template <class T>
+int linear_solve(SolverState *s, Krylov &k, const TDyNewtonOptions &o, cudaStream_t st, long long *lin_total) {
+  int ierr;
+  if ((ierr = krylov_alloc<T>(s, k))) return ierr;
+  if ((ierr = autotune_spmv<T>(s, k, st))) return ierr;  // uses b and v as scratch before they are set
+  const int n = s->n, ns = s->nseg;
+  cast_kernel<T><<<nblk(s->nnz, 256), 256, 0, st>>>(s->nnz, s->J, (T *)k.Jv);
+  line_factor_kernel<T><<<nblk(s->nlines, 128), 128, 0, st>>>(s->nlines, s->line_off, s->pos_d, s->pos_lo, s->pos_hi,
+                                                               s->J, (T *)k.la, (T *)k.lcp, (T *)k.linv);
+  init_kernel<T><<<nblk(n, 256), 256, 0, st>>>(n, s->cell_seg, s->newt_active, s->F, (T *)k.b, (T *)k.r, (T *)k.r0,
+                                               (T *)k.p, (T *)k.v, (T *)k.y);
+  dot<T>(s, (T *)k.b, (T *)k.b, nullptr, nullptr, S_BNORM2, 0, st);
+  SCUDA(cudaMemsetAsync(s->lin_its, 0, sizeof(int) * ns, st));
+  init_scalars_kernel<<<nblk(ns, 128), 128, 0, st>>>(ns, s->newt_active, s->lin_active, s->lin_its, s->scal);
+  SCUDA(cudaGetLastError());
+  const double tol2 = o.linear_rtol * o.linear_rtol;
+  if (!k.graph || k.graph_stream != st || s->linear_rtol != o.linear_rtol) {
+    if (k.graph) cudaGraphExecDestroy(k.graph);
+    k.graph = nullptr;
+    cudaGraph_t g;
+    SCUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    bicgstab_iteration<T>(s, k, tol2, st);
+    SCUDA(cudaStreamEndCapture(st, &g));
+    cudaError_t e = cudaGraphInstantiate(&k.graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return set_error(TDY_ERR_GPU, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
+    k.graph_stream = st;
+    s->linear_rtol = o.linear_rtol;
+  }
+  std::vector<int> act(ns), its(ns);
+  const int check_every = 8;
+  for (int it = 0; it < o.linear_max_it; it += check_every) {
+    for (int j = 0; j < check_every && it + j < o.linear_max_it; j++) SCUDA(cudaGraphLaunch(k.graph, st));
+    SCUDA(cudaMemcpyAsync(act.data(), s->lin_active, sizeof(int) * ns, cudaMemcpyDeviceToHost, st));
+    SCUDA(cudaStreamSynchronize(st));
+    bool any = false;
+    for (int a : act) any |= (a != 0);
+    if (!any) break;
+  }
+  SCUDA(cudaMemcpyAsync(its.data(), s->lin_its, sizeof(int) * ns, cudaMemcpyDeviceToHost, st));
+  SCUDA(cudaStreamSynchronize(st));
+  for (int v : its) *lin_total += v;
+  return 0;
+}
+
+int solver_init(_p_TDy *t) {
+  if (t->solver) return 0;
+  const MPFAOSetup &su = t->setup;
+  SolverState *s = new SolverState();
+  t->solver = s;
+  s->n = t->mesh.nc;
+  s->nnz = (int)su.colidx.size();
+  // instances: the mesh blocks; lines: the columns of each block, bottom to top
+  std::vector<int> seg_off(1, 0), cell_seg(s->n), line_off(1, 0), line_cells, pd, plo, phi;
+  line_cells.reserve(s->n);
+  auto find = [&](int i, int j) {
+    const int *b = su.colidx.data() + su.rowptr[i], *e = su.colidx.data() + su.rowptr[i + 1];
+    const int *q = std::lower_bound(b, e, j);
+    return (q != e && *q == j) ? (int)(q - su.colidx.data()) : -1;
+  };
+  int c0 = 0;
+  for (const ExtrudedInput &blk : t->mesh_blocks) {
+    const int nc2 = blk.nc2, nl = blk.nlayers;
+    for (int c2 = 0; c2 < nc2; c2++) {
+      for (int k = 0; k < nl; k++) {
+        const int i = c0 + k * nc2 + c2;
+        line_cells.push_back(i);
+        pd.push_back(find(i, i));
+        plo.push_back(k > 0 ? find(i, i - nc2) : -1);
+        phi.push_back(k + 1 < nl ? find(i, i + nc2) : -1);
+        if (pd.back() < 0) return set_error(TDY_ERR_LIB, "solver: missing diagonal of cell %d", i);
+      }
+      line_off.push_back((int)line_cells.size());
+    }
+    for (int i = c0; i < c0 + nc2 * nl; i++) cell_seg[i] = (int)seg_off.size() - 1;
+    c0 += nc2 * nl;
+    seg_off.push_back(c0);
+  }
+  if (c0 != s->n) return set_error(TDY_ERR_LIB, "solver: blocks cover %d of %d cells", c0, s->n);
+  s->nseg = (int)seg_off.size() - 1;
+  s->nlines = (int)line_off.size() - 1;
+  s->h_seg_off = seg_off;
+  int ierr;
+  if ((ierr = sup(s, &s->rowptr, su.rowptr))) return ierr;
+  if ((ierr = sup(s, &s->colidx, su.colidx))) return ierr;
+  if ((ierr = sup(s, &s->seg_off, seg_off))) return ierr;
+  if ((ierr = sup(s, &s->cell_seg, cell_seg))) return ierr;
+  if ((ierr = sup(s, &s->line_off, line_off))) return ierr;
+  if ((ierr = sup(s, &s->line_cells, line_cells))) return ierr;
+  if ((ierr = sup(s, &s->pos_d, pd))) return ierr;
+  if ((ierr = sup(s, &s->pos_lo, plo))) return ierr;
+  if ((ierr = sup(s, &s->pos_hi, phi))) return ierr;
+  if ((ierr = salloc(s, &s->x, s->n))) return ierr;
+  if ((ierr = salloc(s, &s->xb, s->n))) return ierr;
+  if ((ierr = salloc(s, &s->lam, s->nseg))) return ierr;
+  if ((ierr = salloc(s, &s->trial, s->nseg))) return ierr;
+  if ((ierr = salloc(s, &s->commit, s->nseg))) return ierr;
+  if ((ierr = salloc(s, &s->F, s->n))) return ierr;
+  if ((ierr = salloc(s, &s->J, s->nnz))) return ierr;
+  if ((ierr = salloc(s, &s->fn2, s->nseg))) return ierr;
+  if ((ierr = salloc(s, &s->scal, (size_t)S_NSCAL * s->nseg))) return ierr;
+  if ((ierr = salloc(s, &s->newt_active, s->nseg))) return ierr;
+  if ((ierr = salloc(s, &s->lin_active, s->nseg))) return ierr;
+  if ((ierr = salloc(s, &s->lin_its, s->nseg))) return ierr;
+  return 0;
+}
+
+}  // namespace
+
+void device_solver_destroy(_p_TDy *t) {
+  delete t->solver;
+  t->solver = nullptr;
+}
+
+int device_num_instances(_p_TDy *t) { return (int)t->mesh_blocks.size(); }
+
+int device_be_solve(_p_TDy *t, double dt, double *dU, const TDyNewtonOptions &o, TDyNewtonStats *stats,
+                    int *inst_its, double *inst_rel, void *stream) {
+  int ierr;
+  if ((ierr = solver_init(t))) {
+    device_solver_destroy(t);
+    return ierr;
+  }
+  SolverState *s = t->solver;
+  // a capturable stream: the caller's, else the handle's own
+  cudaStream_t st = (cudaStream_t)(stream ? stream : device_default_stream(t));
+  const int n = s->n, ns = s->nseg;
+  t->dtime = dt;
+  if ((ierr = device_presolve(t, dU, st))) return ierr;
+  SCUDA(cudaMemcpyAsync(s->x, dU, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+  SCUDA(cudaMemcpyAsync(s->xb, dU, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+  std::vector<double> f0(ns, 0.0), fn(ns, 0.0), g2(ns, 0.0), lam(ns, 1.0);
+  std::vector<int> act(ns, 1), its(ns, 0), trial(ns, 0), commit(ns, 0), step_conv(ns, 0);
+  std::vector<double> y2(ns, 0.0), x2(ns, 0.0);
+  long long lin_total = 0;
+  // F and J at x (= xb for every instance after each evaluation below), and
+  // the squared per-instance residual norms into g2
+  auto evaluate = [&]() -> int {
+    int e;
+    if ((e = device_eval(t, FORM_SNES, 0.0, s->x, nullptr, 0.0, s->F, s->J, st))) return e;
+    seg_dot_kernel<double, double><<<ns, 256, 0, st>>>(s->seg_off, s->F, s->F, nullptr, nullptr, s->fn2, nullptr);
+    SCUDA(cudaGetLastError());
+    SCUDA(cudaMemcpyAsync(g2.data(), s->fn2, sizeof(double) * ns, cudaMemcpyDeviceToHost, st));
+    SCUDA(cudaStreamSynchronize(st));
+    return 0;
+  };
+  if ((ierr = evaluate())) return ierr;
+  for (int g = 0; g < ns; g++) f0[g] = fn[g] = std::sqrt(g2[g]);
+  const double alpha = 1e-4;  // sufficient-decrease constant of PETSc's backtracking line search
+  const int max_backtracks = 12;
+  for (int it = 0;; it++) {
+    bool any = false;
+    for (int g = 0; g < ns; g++) {
+      if (act[g]) {
+        const bool done = !(fn[g] > o.atol) || fn[g] <= o.rtol * f0[g];
+        if (done || it == o.max_it) act[g] = 0;  // converged, or out of iterations (reported below)
+        else its[g] = it + 1;
+      }
+      any |= act[g] != 0;
+    }
+    if (!any) break;
+    SCUDA(cudaMemcpyAsync(s->newt_active, act.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, st));
+    const void *y;
+    if (o.linear_fp32) {
+      ierr = linear_solve<float>(s, s->k32, o, st, &lin_total);
+      y = s->k32.y;
+    } else {
+      ierr = linear_solve<double>(s, s->k64, o, st, &lin_total);
+      y = s->k64.y;
+    }
+    if (ierr) return ierr;
+    // backtracking per instance: accept when ||F(x - lam y)||^2 <= (1 - 2 alpha lam) ||F(x)||^2
+    // (initial slope -||F||^2 of the Newton direction), else a quadratic fit of
+    // lam clamped to [0.1 lam, 0.5 lam] (PETSc SNESLineSearchApply_BT)
+    for (int g = 0; g < ns; g++) {
+      trial[g] = act[g];
+      lam[g] = 1.0;
+    }
+    for (int ls = 0; ls <= max_backtracks; ls++) {
+      SCUDA(cudaMemcpyAsync(s->trial, trial.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, st));
+      SCUDA(cudaMemcpyAsync(s->lam, lam.data(), sizeof(double) * ns, cudaMemcpyHostToDevice, st));
+      if (o.linear_fp32)
+        trial_kernel<float><<<nblk(n, 256), 256, 0, st>>>(n, s->cell_seg, s->trial, s->lam, (const float *)y, s->xb,
+                                                          s->x);
+      else
+        trial_kernel<double><<<nblk(n, 256), 256, 0, st>>>(n, s->cell_seg, s->trial, s->lam, (const double *)y, s->xb,
+                                                           s->x);
+      if ((ierr = evaluate())) return ierr;
+      bool pending = false;
+      for (int g = 0; g < ns; g++) {
+        commit[g] = 0;
+        if (!trial[g]) continue;
+        const double f = fn[g] * fn[g], gg = g2[g];
+        if ((std::isfinite(gg) && gg <= (1.0 - 2.0 * alpha * lam[g]) * f) || ls == max_backtracks) {
+          commit[g] = 1;  // accepted (or the smallest step after the last backtrack)
+          trial[g] = 0;
+          fn[g] = std::sqrt(gg);
+        } else {
+          const double slope = -f;
+          double lt = std::isfinite(gg) ? -slope * lam[g] * lam[g] / (gg - f - 2.0 * slope * lam[g]) : 0.0;
+          lt = std::min(lt, 0.5 * lam[g]);
+          lam[g] = (lt <= 0.1 * lam[g]) ? 0.1 * lam[g] : lt;
+          pending = true;
+        }
+      }
+      SCUDA(cudaMemcpyAsync(s->commit, commit.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, st));
+      commit_kernel<<<nblk(n, 256), 256, 0, st>>>(n, s->cell_seg, s->commit, s->x, s->xb);
+      SCUDA(cudaGetLastError());
+      if (!pending) break;
+    }
+    // every instance now has x == xb, so F and J hold the accepted states.
+    // Step test (SNESConvergedDefault): ||lam y|| < stol ||x|| per instance.
+    if (o.stol > 0.0) {
+      if (o.linear_fp32)
+        seg_dot_kernel<float, float><<<ns, 256, 0, st>>>(s->seg_off, (const float *)y, (const float *)y, nullptr,
+                                                         nullptr, s->fn2, nullptr);
+      else
+        seg_dot_kernel<double, double><<<ns, 256, 0, st>>>(s->seg_off, (const double *)y, (const double *)y, nullptr,
+                                                           nullptr, s->fn2, nullptr);
+      seg_dot_kernel<double, double><<<ns, 256, 0, st>>>(s->seg_off, s->xb, s->xb, nullptr, nullptr,
+                                                         s->scal + (size_t)S_T2 * ns, nullptr);
+      SCUDA(cudaGetLastError());
+      SCUDA(cudaMemcpyAsync(y2.data(), s->fn2, sizeof(double) * ns, cudaMemcpyDeviceToHost, st));
+      SCUDA(cudaMemcpyAsync(x2.data(), s->scal + (size_t)S_T2 * ns, sizeof(double) * ns, cudaMemcpyDeviceToHost, st));
+      SCUDA(cudaStreamSynchronize(st));
+      for (int g = 0; g < ns; g++)
+        if (act[g] && lam[g] * std::sqrt(y2[g]) < o.stol * std::sqrt(x2[g])) {
+          act[g] = 0;
+          step_conv[g] = 1;
+        }
+    }
+  }
+  SCUDA(cudaMemcpyAsync(dU, s->xb, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+  SCUDA(cudaStreamSynchronize(st));
+  int conv = 0, maxit = 0;
+  double worst = 0.0;
+  for (int g = 0; g < ns; g++) {
+    const double rel = f0[g] > 0.0 ? fn[g] / f0[g] : 0.0;
+    const bool ok = !(fn[g] > o.atol) || rel <= o.rtol || step_conv[g];
+    conv += ok ? 1 : 0;
+    worst = std::max(worst, rel);
+    maxit = std::max(maxit, its[g]);
+    if (inst_its) inst_its[g] = its[g];
+    if (inst_rel) inst_rel[g] = rel;
+  }
+  if (stats) {
+    stats->newton_iterations = maxit;
+    stats->linear_iterations = lin_total;
+    stats->converged = conv;
+    stats->ninstances = ns;
+    stats->max_rel_residual = worst;
+  }
+  return 0;
+}
+
+}  // namespace tdy

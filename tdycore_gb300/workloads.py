@@ -92,7 +92,7 @@ def box_column(nx, ny, nz, *, density=WATER_DENSITY_EXPONENTIAL, gmatrix=0, bc_t
 
 
 def top_dirichlet_types(ztop, tol=1e-9):
-    return lambda x, y, z: DIRICHLET_BC if z > ztop - tol else NEUMANN_BC
+    return lambda x, y, z: np.where(np.asarray(z) > ztop - tol, DIRICHLET_BC, NEUMANN_BC)
 
 
 def hydrostatic_box(n=10, rho=998.2):
@@ -211,3 +211,82 @@ def wedge_extruded(npts=200, nlayers=4, lx=1000.0, ly=1000.0, seed_offset=0, dz_
     zc = 0.5 * (levels[layer] + levels[layer + 1])
     U = hydrostatic(zc, ztop, 998.0) + _rng(13 + seed_offset).normal(0.0, 3e3, nc)
     return t, U, {"workload": f"wedge_{tris.shape[0]}tri_{nlayers}layers", "ncells": nc}
+
+
+def batched_columns(ninst=4096, seed_offset=0, cell=1.0, gap=1.0, top_excess=2000.0):
+    """Independent hexahedral subdomains in one handle (TDySetExtrudedMeshes):
+    nx, ny ~ U{1..8}, nz ~ U{10..100}, layer thickness ~ U(0.05, 0.5) m per
+    instance, horizontal cells of ``cell`` m; per instance a homogeneous
+    isotropic k (log10 ~ N(-12, 1) m^2), porosity ~ U(0.05, 0.35), van
+    Genuchten alpha ~ logU(1e-5, 1e-3) 1/Pa and m ~ U(0.2, 0.6), Sr 0.15.
+    Instances sit side by side along x (``gap`` m apart).  Start: hydrostatic
+    (rho 998 kg/m^3) with the water table at 40 % of the depth from the top,
+    plus N(0, 10 Pa) noise;
+    boundary: on each instance's top face Dirichlet at its hydrostatic
+    pressure plus ``top_excess`` Pa (infiltration), no flow elsewhere.
+    Returns (tdy, U0, info)."""
+    r = _rng(20 + seed_offset)
+    nx = r.integers(1, 9, ninst)
+    ny = r.integers(1, 9, ninst)
+    nz = r.integers(10, 101, ninst)
+    dz = r.uniform(0.05, 0.5, ninst)
+    blocks, x0 = [], 0.0
+    xs, ztops = [], []
+    for b in range(ninst):
+        xy, quads = structured_surface(int(nx[b]), int(ny[b]), cell * nx[b], cell * ny[b])
+        xy[:, 0] += x0
+        xs.append(x0)
+        x0 += cell * nx[b] + gap
+        depth = dz[b] * nz[b]
+        z = layered_z(xy.shape[0], int(nz[b]), depth)
+        ztops.append(depth)
+        blocks.append((xy, quads, z))
+    ncell = (nx * ny * nz).astype(np.int64)
+    t = create_richards_mpfao()
+    t.set_extruded_meshes(blocks)
+    t.set_from_options()
+    rp = _rng(21 + seed_offset)
+    k = np.repeat(10.0 ** rp.normal(-12.0, 1.0, ninst), ncell)
+    K = np.zeros((k.size, 9))
+    K[:, 0] = K[:, 4] = K[:, 8] = k
+    t.set_permeability_values(K)
+    poro = np.repeat(rp.uniform(0.05, 0.35, ninst), ncell)
+    t.set_porosity_values(poro)
+    m = np.repeat(rp.uniform(0.2, 0.6, ninst), ncell)
+    alpha = np.repeat(10.0 ** rp.uniform(-5.0, -3.0, ninst), ncell)
+    t.set_vangenuchten_values(m, alpha)
+    t.set_mualem_values(m)
+    t.set_constant_residual_saturation(0.15)
+    t.set_water_density_type(WATER_DENSITY_CONSTANT)
+    xs, ztops = np.asarray(xs), np.asarray(ztops)
+
+    def which(x):
+        # instance of a boundary face by its x: split at the middle of the gaps
+        # (a face centroid on an instance's edge may round to either side of it)
+        return np.clip(np.searchsorted(xs - 0.5 * gap, np.asarray(x), side="right") - 1, 0, ninst - 1)
+
+    t.set_boundary_pressure_type_function(
+        lambda x, y, z: np.where(np.asarray(z) > ztops[which(x)] - 1e-9, DIRICHLET_BC, NEUMANN_BC))
+    ptop = PREF + 998.0 * GRAVITY * (0.6 * ztops - ztops) + top_excess
+    t.set_boundary_pressure_function(lambda x, y, z: ptop[which(x)])
+    # cell-centre depths: layer centres of each instance
+    U = np.empty(int(ncell.sum()))
+    o = 0
+    for b in range(ninst):
+        kk = np.arange(int(nz[b]))
+        zc = (kk + 0.5) * dz[b]
+        depth = dz[b] * nz[b]
+        table = 0.6 * depth
+        p = PREF + 998.0 * GRAVITY * (table - zc)
+        U[o:o + ncell[b]] = np.repeat(p, nx[b] * ny[b])
+        o += ncell[b]
+    # 10 Pa of noise: an exactly hydrostatic state puts every vertical face at
+    # an upwinding tie (T.P + rho G = 0 up to rounding)
+    U += _rng(22 + seed_offset).normal(0.0, 10.0, U.size)
+    info = {"workload": f"batched_columns_{ninst}", "ninstances": ninst, "ncells": int(ncell.sum()),
+            "seed": MASTER_SEED, "instance_cells": ncell}
+    # the inputs, for building one instance on its own
+    t._blocks = blocks
+    t._props = {"K": K, "poro": poro, "m": m, "alpha": alpha}
+    return t, U, info
+
