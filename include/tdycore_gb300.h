@@ -309,6 +309,8 @@ TDyErrorCode TDyGetLiquidMass(TDy tdy, double *mass);
 /* Setup export for test harnesses (host arrays owned by the handle); the
  * layout is described in tdycore_gb300_setup.h. */
 struct TDyMPFAOSetupView;
+/* With -tdy_mpfao_setup_on_device the interior vertices' Trans is built on
+ * the device; the first call copies it into the host arrays of the view. */
 TDyErrorCode TDyMPFAOGetSetupView(TDy tdy, struct TDyMPFAOSetupView *view);
 
 #ifdef __cplusplus

@@ -864,6 +864,27 @@ TDyErrorCode TDyMPFAOGetSetupView(TDy tdy, struct TDyMPFAOSetupView *v) {
   TDY_CHECK_HANDLE(tdy);
   TDY_CHECK_SETUP(tdy);
   if (!v) return set_error(TDY_ERR_ARG_NULL, "null view");
+  // With -tdy_mpfao_setup_on_device the interior vertices' Trans exists only
+  // on the device: bring it into the host arrays the view points at, once.
+  if (tdy->opt.setup_on_device && tdy->dev && !tdy->trans_on_host) {
+    MPFAOSetup &su = tdy->setup;
+    std::vector<double> Tc;
+    int ierr = device_download_tc(tdy, Tc);
+    if (ierr) return ierr;
+    const long long P = su.nCpad;
+    for (int k = 0; k < su.nC; k++) {
+      const int vtx = su.canon_vertex[k];
+      const int r0 = su.v_row_off[vtx], c0 = su.v_col_off[vtx];
+      std::array<int, 8> oc;
+      std::array<int, 12> cr;
+      if (!canonical_layout(tdy->mesh, vtx, &su.col_ext[c0], &su.row_lup[r0], &su.row_ldn[r0], oc, cr))
+        return set_error(TDY_ERR_LIB, "vertex %d lost its canonical layout", vtx);
+      double *T = &su.trans[su.v_trans_off[vtx]];
+      for (int rc = 0; rc < 12; rc++)
+        for (int o = 0; o < 8; o++) T[cr[rc] * 8 + oc[o]] = Tc[(rc * 8 + o) * P + k];
+    }
+    tdy->trans_on_host = true;
+  }
   const Mesh &m = tdy->mesh;
   const MPFAOSetup &s = tdy->setup;
   static thread_local std::vector<int> face_nverts;

@@ -31,6 +31,8 @@ int device_transient_variable_host(_p_TDy *t, const double *U, double *C, double
 // DAE form: U, U_t, R interleaved [P, M] per cell (2 * ncells values).
 int device_eval_dae_host(_p_TDy *t, double time, const double *U2, const double *Ut2, double *R2);
 void *device_default_stream(_p_TDy *t);
+// copies the device's canonical-vertex Trans (96 x nCpad) to the host
+int device_download_tc(_p_TDy *t, std::vector<double> &Tc);
 // Backward-Euler Newton solve of every instance (tdy_solver.cu).
 int device_be_solve(_p_TDy *t, double dt, double *dU, const TDyNewtonOptions &o, TDyNewtonStats *stats,
                     int *inst_its, double *inst_rel, void *stream);

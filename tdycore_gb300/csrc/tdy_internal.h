@@ -7,6 +7,7 @@
 // uploaded to the device in flat structure-of-arrays form.
 #pragma once
 
+#include <array>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -174,6 +175,10 @@ struct MPFAOSetup {
 };
 
 int mpfao_setup(const Options &opt, const Mesh &m, const Materials &mat, const Boundary &bnd, MPFAOSetup &s);
+// Octant of each local cell and canonical row of each vertex row of a vertex
+// with 8 cells and 12 flux rows; false when it does not fit the layout.
+bool canonical_layout(const Mesh &m, int v, const int *cells, const int *lup, const int *ldn,
+                      std::array<int, 8> &oc, std::array<int, 12> &cr);
 
 // Canonical interior-hex row order: row r joins octants kCanonUp[r] (lower
 // side, the face's first cell) and kCanonDn[r] = kCanonUp[r] | (1 << (r / 4)).
@@ -232,6 +237,7 @@ struct _p_TDy {
   std::vector<double> U_prev;
   tdy::DeviceState *dev = nullptr;
   tdy::SolverState *solver = nullptr;  // device Newton solver, on first use
+  bool trans_on_host = false;          // device-built Trans copied into setup.trans
 };
 
 enum : unsigned {

@@ -1045,6 +1045,13 @@ int device_eval(_p_TDy *t, int form, double time, const double *dU, const double
 
 void *device_default_stream(_p_TDy *t) { return t->dev ? (void *)t->dev->stream : nullptr; }
 
+int device_download_tc(_p_TDy *t, std::vector<double> &Tc) {
+  const DeviceState *d = t->dev;
+  Tc.resize(96 * (size_t)t->setup.nCpad);
+  CUDA_TRY(cudaMemcpy(Tc.data(), d->a.Tc, sizeof(double) * Tc.size(), cudaMemcpyDeviceToHost));
+  return 0;
+}
+
 int device_set_timers(_p_TDy *t, int on) {
   DeviceState *d = t->dev;
   if (on && !d->ev[0])

@@ -268,6 +268,8 @@ double face_perm_value(const Mesh &m, const Materials &mat, int method, int f, c
   return (kup * kdn) / (wt_up * kdn + (1.0 - wt_up) * kup);
 }
 
+}  // namespace
+
 // Octant layout of a vertex with 8 cells and 12 flux rows: the octant of each
 // local cell from its centroid relative to the vertex (bit 0 x, bit 1 y,
 // bit 2 z) and the canonical row (kCanonUp/kCanonDn) of each vertex row.
@@ -303,7 +305,6 @@ bool canonical_layout(const Mesh &m, int v, const int *cells, const int *lup, co
   return true;
 }
 
-}  // namespace
 
 int mpfao_setup(const Options &opt, const Mesh &m, const Materials &mat, const Boundary &bnd, MPFAOSetup &s) {
   s = MPFAOSetup();

@@ -629,7 +629,10 @@ int device_be_solve(_p_TDy *t, double dt, double *dU, const TDyNewtonOptions &o,
       if (!pending) break;
     }
     // every instance now has x == xb, so F and J hold the accepted states.
-    // Step test (SNESConvergedDefault): ||lam y|| < stol ||x|| per instance.
+    // Step test (SNESConvergedDefault): ||y|| < stol ||x|| per instance, with
+    // y the full Newton step (PETSc's backtracking line search reports the
+    // norm of the step before its lambda scaling), so a step cut short by the
+    // line search does not count as convergence.
     if (o.stol > 0.0) {
       if (o.linear_fp32)
         seg_dot_kernel<float, float><<<ns, 256, 0, st>>>(s->seg_off, (const float *)y, (const float *)y, nullptr,
@@ -644,7 +647,7 @@ int device_be_solve(_p_TDy *t, double dt, double *dU, const TDyNewtonOptions &o,
       SCUDA(cudaMemcpyAsync(x2.data(), s->scal + (size_t)S_T2 * ns, sizeof(double) * ns, cudaMemcpyDeviceToHost, st));
       SCUDA(cudaStreamSynchronize(st));
       for (int g = 0; g < ns; g++)
-        if (act[g] && lam[g] * std::sqrt(y2[g]) < o.stol * std::sqrt(x2[g])) {
+        if (act[g] && std::sqrt(y2[g]) < o.stol * std::sqrt(x2[g])) {
           act[g] = 0;
           step_conv[g] = 1;
         }

@@ -162,3 +162,26 @@ def test_device_built_transmissibility(name):
     rowmax = np.maximum.reduceat(Jm, t.rowptr[:-1])
     row_of = np.repeat(np.arange(t.ncells), np.diff(t.rowptr))
     assert_close(J, Jr, np.maximum(Jm, 1e-16 * rowmax[row_of]), J_TOL, f"{name} SNES Jacobian, device-built Trans")
+
+
+@pytest.mark.parametrize("name", ["spe10_small", "tpf_dirichlet", "mixed_curves"])
+def test_device_built_trans_in_setup_view(name):
+    """The setup view of a handle with device-built Trans holds the device
+    values; they equal the host-built ones to rounding of the row scale."""
+    parity_cases.EXTRA_OPTIONS = "-tdy_mpfao_setup_on_device"
+    try:
+        t, _, _, _ = CASES[name]()
+    finally:
+        parity_cases.EXTRA_OPTIONS = ""
+    t.setup()
+    th, _, _, _ = CASES[name]()
+    th.setup(host_only=True)
+    vd, vh = t.setup_view(), th.setup_view()
+    Td, Th = vd["trans"], vh["trans"]
+    assert Td.shape == Th.shape
+    for v in range(vh["nverts"]):
+        a, b = vh["v_trans_off"][v], vh["v_trans_off"][v + 1]
+        if a == b:
+            continue
+        scale = np.abs(Th[a:b]).max()
+        assert np.all(np.abs(Td[a:b] - Th[a:b]) <= 1e-13 * scale), v
