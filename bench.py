@@ -323,6 +323,35 @@ def batched_config4(ninst=4096, sample=64, dt=3600.0):
     }
 
 
+def serving_config5(nreq=160, rate=80.0, slots=32):
+    """Config 5: Poisson arrivals of column/subdomain requests (5 % of them
+    64 x 64 x 50 cells), 24 hourly backward-Euler steps each with top-flux
+    forcing, state resident on the device, admission by HBM footprint against
+    150 GB; continuous batching (``slots`` requests in flight, FP32 inner
+    solves) next to plain FP64 one-at-a-time serving of the same requests."""
+    from tdycore_gb300 import serving as S
+
+    out = {}
+    for name, kw in (("continuous_fp32", {"slots": slots, "fp32": True}),
+                     ("one_at_a_time_fp64", {"slots": 1, "fp32": False})):
+        reqs = S.make_requests(nreq, rate_per_s=rate, nsteps=24, large_fraction=0.05, seed=0)
+        srv = S.Server(hbm_budget_bytes=150e9, **kw)
+        t0 = time.perf_counter()
+        done = srv.run(reqs)
+        wall = time.perf_counter() - t0
+        out[name] = S.summary(done, wall)
+        out[name]["peak_requests_in_flight"] = srv.peak_running
+        out[name]["peak_hbm_reserved_GB"] = srv.peak_in_use / 1e9
+        log(f"config 5 {name}: {out[name]}")
+    out["requests"] = nreq
+    out["arrival_rate_per_s"] = rate
+    out["large_requests"] = int(sum((r.nx, r.ny, r.nz) == (64, 64, 50)
+                                    for r in S.make_requests(nreq, rate, 24, 0.05, 0)))
+    c, o = out["continuous_fp32"], out["one_at_a_time_fp64"]
+    out["solves_per_s_ratio"] = c["solves_per_s"] / o["solves_per_s"]
+    return out
+
+
 def cpu_baseline(o, U, budget_s=12.0, threads=None):
     ncells = U.size
     """Oracle F+J (reference loop order, colour-parallel) on the host cores."""
@@ -521,6 +550,12 @@ def run_gpu(args, rank, world, local_rank):
             cfg1 = newton_config1()
         except Exception as e:  # reported, never fatal to the headline line
             cfg1 = {"error": repr(e)}
+        cfg5 = None
+        if args.serve_requests > 0:
+            try:
+                cfg5 = serving_config5(args.serve_requests)
+            except Exception as e:
+                cfg5 = {"error": repr(e)}
         cfg4 = None
         if args.batch_instances > 0:
             try:
@@ -554,6 +589,7 @@ def run_gpu(args, rank, world, local_rank):
             "parity_full_size": parity,
             "config1_newton": cfg1,
             "config4_batched": cfg4,
+            "config5_serving": cfg5,
             "setup_s": {"trans_on_host": info["setup_s"],
                         "trans_on_device": alt["setup_s"] if alt is not None else None,
                         "note": "TDySetup wall time (mesh, materials, interaction regions, layouts, upload); "
@@ -581,6 +617,8 @@ def main():
                     help="smaller grid with the same extents per cell (profiling captures)")
     ap.add_argument("--jacobian-arithmetic", default="DOUBLE_FLOAT", choices=["DOUBLE_FLOAT", "FP64"],
                     help="arithmetic of the Jacobian products at interior hexahedral vertices")
+    ap.add_argument("--serve-requests", type=int, default=160,
+                    help="requests of the serving measurement (0 skips it)")
     ap.add_argument("--batch-instances", type=int, default=4096,
                     help="instances of the batched-solve measurement (0 skips it)")
     ap.add_argument("--profile", action="store_true",

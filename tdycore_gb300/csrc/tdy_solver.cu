@@ -64,6 +64,9 @@ struct SolverState {
   double *x = nullptr, *xb = nullptr, *F = nullptr, *J = nullptr, *fn2 = nullptr, *scal = nullptr, *lam = nullptr;
   int *trial = nullptr, *commit = nullptr;
   int *newt_active = nullptr, *lin_active = nullptr, *lin_its = nullptr;
+  int nchunks = 0;
+  int *chunk_off = nullptr, *seg_chunk = nullptr;  // chunks of the per-instance reductions
+  double *part = nullptr, *part2 = nullptr;
   double linear_rtol = -1.0;
   Krylov k32, k64;
   std::vector<void *> allocs;
@@ -101,14 +104,18 @@ __global__ void cast_kernel(long long n, const double *a, T *b) {
   if (i < n) b[i] = (T)a[i];
 }
 
-// out[s] = sum over instance s of a*b (and out2[s] of c*d), FP64 accumulation;
-// one block per instance
+// Per-instance dot products in two deterministic passes: one block per chunk
+// of at most kChunk cells (chunks counted from each instance's first cell, so
+// an instance is reduced the same way alone and in a batch), then one thread
+// per instance adding its chunks in order.
+constexpr int kChunk = 4096;
+
 template <class TA, class TB>
-__global__ void __launch_bounds__(256) seg_dot_kernel(const int *seg_off, const TA *a, const TB *b, const TA *c,
-                                                      const TB *d, double *out, double *out2) {
+__global__ void __launch_bounds__(256) chunk_dot_kernel(const int *chunk_off, const TA *a, const TB *b, const TA *c,
+                                                        const TB *d, double *part, double *part2) {
   __shared__ double sh[2][256];
-  const int s = blockIdx.x;
-  const int i0 = seg_off[s], i1 = seg_off[s + 1];
+  const int ch = blockIdx.x;
+  const int i0 = chunk_off[ch], i1 = chunk_off[ch + 1];
   double acc = 0.0, acc2 = 0.0;
   for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
     acc += (double)a[i] * (double)b[i];
@@ -125,9 +132,22 @@ __global__ void __launch_bounds__(256) seg_dot_kernel(const int *seg_off, const 
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    out[s] = sh[0][0];
-    if (c) out2[s] = sh[1][0];
+    part[ch] = sh[0][0];
+    if (c) part2[ch] = sh[1][0];
   }
+}
+
+__global__ void chunk_sum_kernel(int nseg, const int *seg_chunk, const double *part, const double *part2, double *out,
+                                 double *out2) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nseg) return;
+  double acc = 0.0, acc2 = 0.0;
+  for (int k = seg_chunk[s]; k < seg_chunk[s + 1]; k++) {
+    acc += part[k];
+    if (out2) acc2 += part2[k];
+  }
+  out[s] = acc;
+  if (out2) out2[s] = acc2;
 }
 
 // y = A x over the CSR pattern with TPR threads per row
@@ -326,10 +346,17 @@ int spmv(SolverState *s, const Krylov &k, const T *x, T *y, cudaStream_t st) {
   return 0;
 }
 
+template <class TA, class TB>
+void seg_dot(SolverState *s, const TA *a, const TB *b, const TA *c, const TB *d, double *out, double *out2,
+             cudaStream_t st) {
+  chunk_dot_kernel<TA, TB><<<s->nchunks, 256, 0, st>>>(s->chunk_off, a, b, c, d, s->part, s->part2);
+  chunk_sum_kernel<<<nblk(s->nseg, 128), 128, 0, st>>>(s->nseg, s->seg_chunk, s->part, s->part2, out,
+                                                       c ? out2 : nullptr);
+}
+
 template <class T>
 int dot(SolverState *s, const T *a, const T *b, const T *c, const T *d, int slot1, int slot2, cudaStream_t st) {
-  seg_dot_kernel<T, T><<<s->nseg, 256, 0, st>>>(s->seg_off, a, b, c, d, s->scal + (size_t)slot1 * s->nseg,
-                                                 c ? s->scal + (size_t)slot2 * s->nseg : nullptr);
+  seg_dot<T, T>(s, a, b, c, d, s->scal + (size_t)slot1 * s->nseg, c ? s->scal + (size_t)slot2 * s->nseg : nullptr, st);
   return 0;
 }
 
@@ -499,11 +526,21 @@ int solver_init(_p_TDy *t) {
   if (c0 != s->n) return set_error(TDY_ERR_LIB, "solver: blocks cover %d of %d cells", c0, s->n);
   s->nseg = (int)seg_off.size() - 1;
   s->nlines = (int)line_off.size() - 1;
+  std::vector<int> chunk_off(1, 0), seg_chunk(1, 0);
+  for (int g = 0; g < s->nseg; g++) {
+    for (int i = seg_off[g]; i < seg_off[g + 1]; i += kChunk) chunk_off.push_back(std::min(i + kChunk, seg_off[g + 1]));
+    seg_chunk.push_back((int)chunk_off.size() - 1);
+  }
+  s->nchunks = (int)chunk_off.size() - 1;
   s->h_seg_off = seg_off;
   int ierr;
   if ((ierr = sup(s, &s->rowptr, su.rowptr))) return ierr;
   if ((ierr = sup(s, &s->colidx, su.colidx))) return ierr;
   if ((ierr = sup(s, &s->seg_off, seg_off))) return ierr;
+  if ((ierr = sup(s, &s->chunk_off, chunk_off))) return ierr;
+  if ((ierr = sup(s, &s->seg_chunk, seg_chunk))) return ierr;
+  if ((ierr = salloc(s, &s->part, s->nchunks))) return ierr;
+  if ((ierr = salloc(s, &s->part2, s->nchunks))) return ierr;
   if ((ierr = sup(s, &s->cell_seg, cell_seg))) return ierr;
   if ((ierr = sup(s, &s->line_off, line_off))) return ierr;
   if ((ierr = sup(s, &s->line_cells, line_cells))) return ierr;
@@ -558,7 +595,7 @@ int device_be_solve(_p_TDy *t, double dt, double *dU, const TDyNewtonOptions &o,
   auto evaluate = [&]() -> int {
     int e;
     if ((e = device_eval(t, FORM_SNES, 0.0, s->x, nullptr, 0.0, s->F, s->J, st))) return e;
-    seg_dot_kernel<double, double><<<ns, 256, 0, st>>>(s->seg_off, s->F, s->F, nullptr, nullptr, s->fn2, nullptr);
+    seg_dot<double, double>(s, s->F, s->F, nullptr, nullptr, s->fn2, nullptr, st);
     SCUDA(cudaGetLastError());
     SCUDA(cudaMemcpyAsync(g2.data(), s->fn2, sizeof(double) * ns, cudaMemcpyDeviceToHost, st));
     SCUDA(cudaStreamSynchronize(st));
@@ -635,13 +672,10 @@ int device_be_solve(_p_TDy *t, double dt, double *dU, const TDyNewtonOptions &o,
     // line search does not count as convergence.
     if (o.stol > 0.0) {
       if (o.linear_fp32)
-        seg_dot_kernel<float, float><<<ns, 256, 0, st>>>(s->seg_off, (const float *)y, (const float *)y, nullptr,
-                                                         nullptr, s->fn2, nullptr);
+        seg_dot<float, float>(s, (const float *)y, (const float *)y, nullptr, nullptr, s->fn2, nullptr, st);
       else
-        seg_dot_kernel<double, double><<<ns, 256, 0, st>>>(s->seg_off, (const double *)y, (const double *)y, nullptr,
-                                                           nullptr, s->fn2, nullptr);
-      seg_dot_kernel<double, double><<<ns, 256, 0, st>>>(s->seg_off, s->xb, s->xb, nullptr, nullptr,
-                                                         s->scal + (size_t)S_T2 * ns, nullptr);
+        seg_dot<double, double>(s, (const double *)y, (const double *)y, nullptr, nullptr, s->fn2, nullptr, st);
+      seg_dot<double, double>(s, s->xb, s->xb, nullptr, nullptr, s->scal + (size_t)S_T2 * ns, nullptr, st);
       SCUDA(cudaGetLastError());
       SCUDA(cudaMemcpyAsync(y2.data(), s->fn2, sizeof(double) * ns, cudaMemcpyDeviceToHost, st));
       SCUDA(cudaMemcpyAsync(x2.data(), s->scal + (size_t)S_T2 * ns, sizeof(double) * ns, cudaMemcpyDeviceToHost, st));

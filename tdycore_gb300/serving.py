@@ -1,0 +1,227 @@
+"""Continuous-batching request server over the device Newton solver.
+
+Each request is an independent Richards problem: a hexahedral soil column or
+small 3-D subdomain with its own parameters, advanced ``nsteps`` hourly
+backward-Euler steps with a top-flux forcing per step (a source in the top
+layer, rho * q * A kg/s per top cell).  Its state stays on the device for
+the whole request.
+
+Serving is continuous: a request that arrives while others are on the GPU is
+admitted as soon as a slot and enough of the HBM budget are free, and its
+steps overlap on the device with those of the requests already running (each
+request owns a handle, hence its own CUDA stream and device buffers, and is
+driven by a worker thread; the C-ABI calls release the interpreter lock).
+Requests never share device state, and every kernel is deterministic, so a
+request's result is the same alone and in any mix.
+
+No reference counterpart: TDycore runs one problem per process through
+PETSc.
+"""
+from __future__ import annotations
+
+import threading
+import time
+from concurrent.futures import ThreadPoolExecutor
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import NEUMANN_BC, WATER_DENSITY_CONSTANT, create_richards_mpfao, options_clear
+from .workloads import GRAVITY, PREF, layered_z, structured_surface
+
+RHO = 998.0  # constant water density of the EOS used here (kg/m^3)
+
+
+@dataclass
+class Request:
+    rid: int
+    arrival_s: float
+    nx: int
+    ny: int
+    nz: int
+    dz: float
+    k: float          # isotropic permeability (m^2)
+    porosity: float
+    alpha: float      # van Genuchten alpha (1/Pa)
+    m: float          # van Genuchten / Mualem m
+    forcing: np.ndarray  # top flux per step (m/s, positive into the domain)
+    sr: float = 0.15
+    cell: float = 1.0
+    # filled by the server
+    admitted_s: float = float("nan")
+    finished_s: float = float("nan")
+    U_final: np.ndarray | None = field(default=None, repr=False)
+    newton_its: list = field(default_factory=list)
+    rel_residual: list = field(default_factory=list)
+    converged_steps: int = 0
+    error: str | None = None
+
+    @property
+    def ncells(self) -> int:
+        return self.nx * self.ny * self.nz
+
+    @property
+    def latency_s(self) -> float:
+        return self.finished_s - self.arrival_s
+
+
+def footprint_bytes(ncells: int) -> int:
+    """Device bytes one request holds: state, per-vertex partials, Jacobian
+    in FP64 and FP32, Krylov vectors and mesh arrays (about 2 KB per cell),
+    plus a fixed 16 MB."""
+    return 2048 * ncells + (16 << 20)
+
+
+def build(req: Request):
+    """Handle and initial state of a request: hydrostatic with the water table
+    at 60 % of the height (plus 10 Pa of seeded noise, which keeps vertical
+    faces off exact upwinding ties), no-flow boundaries, forcing as a source."""
+    xy, quads = structured_surface(req.nx, req.ny, req.cell * req.nx, req.cell * req.ny)
+    depth = req.dz * req.nz
+    z = layered_z(xy.shape[0], req.nz, depth)
+    t = create_richards_mpfao()
+    t.set_extruded_meshes([(xy, quads, z)])
+    t.set_from_options()
+    n = req.ncells
+    K = np.zeros((n, 9))
+    K[:, 0] = K[:, 4] = K[:, 8] = req.k
+    t.set_permeability_values(K)
+    t.set_porosity_values(np.full(n, req.porosity))
+    t.set_vangenuchten_values(np.full(n, req.m), np.full(n, req.alpha))
+    t.set_mualem_values(np.full(n, req.m))
+    t.set_constant_residual_saturation(req.sr)
+    t.set_water_density_type(WATER_DENSITY_CONSTANT)
+    t.set_boundary_pressure_type_function(lambda x, y, zz: np.full(np.shape(x), NEUMANN_BC))
+    zc = (np.arange(req.nz) + 0.5) * req.dz
+    p = PREF + RHO * GRAVITY * (0.6 * depth - zc)
+    U0 = np.repeat(p, req.nx * req.ny) + np.random.default_rng(1000 + req.rid).normal(0.0, 10.0, n)
+    top = np.arange((req.nz - 1) * req.nx * req.ny, n, dtype=np.int32)
+    return t, U0, top
+
+
+_opts_lock = threading.Lock()
+_opts_cleared = False
+
+
+def options_clear_once():
+    """Requests read no options; clear the database once per process so a
+    caller's leftovers do not leak into request handles."""
+    global _opts_cleared
+    with _opts_lock:
+        if not _opts_cleared:
+            options_clear()
+            _opts_cleared = True
+
+
+def run_request(req: Request, fp32: bool = True, dt: float = 3600.0, rtol: float = 1e-8):
+    """All steps of one request on the calling thread (its own handle and
+    stream); fills the request's results."""
+    import torch
+
+    options_clear_once()
+    t, U0, top = build(req)
+    t.setup()
+    try:
+        dU = torch.tensor(U0, dtype=torch.float64, device="cuda")
+        torch.cuda.current_stream().synchronize()
+        area = req.cell * req.cell
+        for q in req.forcing:
+            t.set_source_sink_values(np.full(top.size, RHO * q * area), cells=top)
+            stats, its, rel = t.backward_euler_step_device(dU, dt, rtol=rtol, fp32=fp32)
+            req.newton_its.append(int(its[0]))
+            req.rel_residual.append(float(rel[0]))
+            req.converged_steps += int(stats["converged"])
+        req.U_final = dU.cpu().numpy()
+    finally:
+        t.destroy()
+
+
+class Server:
+    """Admits requests in arrival order as slots and HBM budget allow and runs
+    them concurrently (``slots`` worker threads)."""
+
+    def __init__(self, slots: int = 32, hbm_budget_bytes: float = 150e9, fp32: bool = True, dt: float = 3600.0,
+                 runner=None, footprint=footprint_bytes, clock=time.perf_counter):
+        self.slots, self.budget, self.fp32, self.dt = slots, float(hbm_budget_bytes), fp32, dt
+        self.runner = runner or (lambda req: run_request(req, fp32=self.fp32, dt=self.dt))
+        self.footprint = footprint
+        self.clock = clock
+        self.peak_in_use = 0.0
+        self.peak_running = 0
+
+    def run(self, requests):
+        """Serves ``requests`` (their arrival_s relative to the start) and
+        returns them with admission/finish times and results."""
+        reqs = sorted(requests, key=lambda r: r.arrival_s)
+        for r in reqs:
+            if self.footprint(r.ncells) > self.budget:
+                raise ValueError(f"request {r.rid} needs more than the whole HBM budget")
+        lock = threading.Condition()
+        in_use, running = [0.0], [0]
+        start = self.clock()
+
+        def work(r):
+            try:
+                self.runner(r)
+            except Exception as e:  # reported per request
+                r.error = repr(e)
+            finally:
+                with lock:
+                    r.finished_s = self.clock() - start
+                    in_use[0] -= self.footprint(r.ncells)
+                    running[0] -= 1
+                    lock.notify_all()
+
+        i = 0
+        with ThreadPoolExecutor(self.slots) as pool:
+            while i < len(reqs):
+                r = reqs[i]
+                with lock:
+                    now = self.clock() - start
+                    if r.arrival_s > now:
+                        lock.wait(timeout=r.arrival_s - now)
+                        continue
+                    need = self.footprint(r.ncells)
+                    if running[0] >= self.slots or in_use[0] + need > self.budget:
+                        lock.wait(timeout=0.05)
+                        continue
+                    in_use[0] += need
+                    running[0] += 1
+                    self.peak_in_use = max(self.peak_in_use, in_use[0])
+                    self.peak_running = max(self.peak_running, running[0])
+                    r.admitted_s = now
+                pool.submit(work, r)
+                i += 1
+        return reqs
+
+
+def make_requests(n: int, rate_per_s: float, nsteps: int = 24, large_fraction: float = 0.05, seed: int = 0):
+    """Poisson arrivals at ``rate_per_s``; sizes and parameters as the batched
+    instances (nx, ny ~ U{1..8}, nz ~ U{10..100}, dz ~ U(0.05, 0.5) m, log10 k
+    ~ N(-12, 1), porosity ~ U(0.05, 0.35), alpha ~ logU(1e-5, 1e-3), m ~
+    U(0.2, 0.6)), ``large_fraction`` of them 64 x 64 x 50 cells; top flux per
+    step ~ N(0, 1e-7 m/s)."""
+    r = np.random.default_rng(20261203 + seed)
+    t = np.cumsum(r.exponential(1.0 / rate_per_s, n))
+    out = []
+    for i in range(n):
+        large = r.uniform() < large_fraction
+        nx, ny, nz = (64, 64, 50) if large else (int(r.integers(1, 9)), int(r.integers(1, 9)), int(r.integers(10, 101)))
+        out.append(Request(rid=i, arrival_s=float(t[i]), nx=nx, ny=ny, nz=nz, dz=float(r.uniform(0.05, 0.5)),
+                           k=float(10.0 ** r.normal(-12.0, 1.0)), porosity=float(r.uniform(0.05, 0.35)),
+                           alpha=float(10.0 ** r.uniform(-5.0, -3.0)), m=float(r.uniform(0.2, 0.6)),
+                           forcing=r.normal(0.0, 1e-7, nsteps)))
+    return out
+
+
+def summary(reqs, wall_s: float):
+    lat = np.array([r.latency_s for r in reqs if r.error is None])
+    steps = sum(r.converged_steps for r in reqs)
+    total = sum(len(r.forcing) for r in reqs)
+    errs = [f"{r.rid}: {r.error}" for r in reqs if r.error is not None]
+    return {"requests": len(reqs), "errors": len(errs), "error_messages": errs[:3],
+            "p50_latency_s": float(np.percentile(lat, 50)) if lat.size else None,
+            "p99_latency_s": float(np.percentile(lat, 99)) if lat.size else None,
+            "solves_per_s": total / wall_s, "converged_solves": steps, "solves": total,
+            "max_rel_residual": float(max((max(r.rel_residual) for r in reqs if r.rel_residual), default=0.0)),
+            "wall_s": wall_s}

@@ -1,0 +1,72 @@
+"""Continuous-batching server: admission by slots and HBM budget in arrival
+order (CPU, with a stand-in runner), and on the GPU each request's result the
+same alone and in a mix, every step converged."""
+import threading
+import time
+
+import numpy as np
+import pytest
+
+from tdycore_gb300 import serving as S
+
+
+def _requests(n, sizes, gaps):
+    t, out = 0.0, []
+    for i in range(n):
+        t += gaps[i]
+        out.append(S.Request(rid=i, arrival_s=t, nx=1, ny=1, nz=int(sizes[i]), dz=0.1, k=1e-12, porosity=0.3,
+                             alpha=1e-4, m=0.4, forcing=np.zeros(2)))
+    return out
+
+
+def test_admission_respects_slots_budget_and_order():
+    n = 24
+    rng = np.random.default_rng(0)
+    reqs = _requests(n, rng.integers(1, 10, n), rng.uniform(0.0, 0.004, n))
+    live, peak, lock = [0], [0], threading.Lock()
+
+    def runner(r):
+        with lock:
+            live[0] += 1
+            peak[0] = max(peak[0], live[0])
+        time.sleep(0.01 + 0.002 * r.nz)
+        with lock:
+            live[0] -= 1
+
+    fp = lambda nc: 10 * nc  # noqa: E731  budget units per cell
+    srv = S.Server(slots=4, hbm_budget_bytes=100, runner=runner, footprint=fp)
+    done = srv.run(reqs)
+    assert all(r.error is None for r in done)
+    assert peak[0] <= 4 and srv.peak_running <= 4
+    assert srv.peak_in_use <= 100
+    admitted = [r.admitted_s for r in sorted(done, key=lambda r: r.arrival_s)]
+    assert admitted == sorted(admitted), "admission follows arrival order"
+    assert all(r.admitted_s >= r.arrival_s - 1e-9 and r.finished_s > r.admitted_s for r in done)
+    with pytest.raises(ValueError):
+        S.Server(slots=2, hbm_budget_bytes=5, runner=runner, footprint=fp).run(_requests(1, [1], [0.0]))
+
+
+def test_request_generator_statistics():
+    reqs = S.make_requests(400, rate_per_s=50.0, nsteps=24, seed=1)
+    gaps = np.diff([0.0] + [r.arrival_s for r in reqs])
+    assert abs(gaps.mean() - 1 / 50.0) < 0.25 / 50.0
+    large = [r for r in reqs if (r.nx, r.ny, r.nz) == (64, 64, 50)]
+    assert 5 <= len(large) <= 40
+    small = [r for r in reqs if r.nz != 50 or r.nx != 64]
+    assert all(1 <= r.nx <= 8 and 1 <= r.ny <= 8 and 10 <= r.nz <= 100 for r in small)
+    f = np.concatenate([r.forcing for r in reqs])
+    assert abs(f.std() - 1e-7) < 1e-8
+
+
+@pytest.mark.gpu
+def test_same_result_alone_and_in_the_mix():
+    reqs = S.make_requests(8, rate_per_s=400.0, nsteps=3, large_fraction=0.0, seed=5)
+    srv = S.Server(slots=4)
+    mix = srv.run(reqs)
+    assert all(r.error is None for r in mix), [r.error for r in mix]
+    assert all(r.converged_steps == 3 for r in mix)
+    for k in (0, 5):
+        alone = S.make_requests(8, rate_per_s=400.0, nsteps=3, large_fraction=0.0, seed=5)[k]
+        S.run_request(alone)
+        assert np.array_equal(alone.U_final, mix[k].U_final)
+        assert alone.newton_its == mix[k].newton_its
