@@ -49,7 +49,10 @@ namespace tdy {
 
 #define TDY_MAX_ROWS 64
 #define TDY_MAX_NINT 64
-#define TDY_MAX_ROW_NNZ 64
+// Jacobian row length: the gather program stores slots in 8 bits; the
+// generic cell kernel stages 64 rows of this length in shared memory
+// (255 doubles x 64 = 130 KB, within the 227 KB a block may use)
+#define TDY_MAX_ROW_NNZ 255
 
 struct DevArgs {
   int nc, nb, nv;
@@ -802,8 +805,9 @@ int device_setup(_p_TDy *t) {
   const Mesh &m = t->mesh;
   const MPFAOSetup &s = t->setup;
   if (s.max_nrow > TDY_MAX_ROWS || s.max_nint > TDY_MAX_NINT || s.max_row_nnz > TDY_MAX_ROW_NNZ)
-    return set_error(TDY_ERR_SUP, "mesh exceeds kernel limits (rows/vertex %d, cells/vertex %d, row nnz %d; max %d)",
-                     s.max_nrow, s.max_nint, s.max_row_nnz, TDY_MAX_ROWS);
+    return set_error(TDY_ERR_SUP,
+                     "mesh exceeds kernel limits (rows/vertex %d, cells/vertex %d, row nnz %d; max %d, %d, %d)",
+                     s.max_nrow, s.max_nint, s.max_row_nnz, TDY_MAX_ROWS, TDY_MAX_NINT, TDY_MAX_ROW_NNZ);
   int ndev = 0;
   cudaError_t e = cudaGetDeviceCount(&ndev);
   if (e != cudaSuccess || ndev == 0)
@@ -1006,6 +1010,14 @@ static int launch_eval(const DevArgs &a, cudaStream_t st, cudaEvent_t *events) {
       vertex_kernel<false, false><<<cb + gb, 128, canon_smem, st>>>(a, gb);
   }
   if (events) CUDA_TRY(cudaEventRecord(events[2], st));
+  if (cell_smem > 48 * 1024) {
+    // rows longer than 96 entries: opt in to more dynamic shared memory
+    static thread_local size_t granted = 48 * 1024;
+    if (cell_smem > granted) {
+      CUDA_TRY(cudaFuncSetAttribute(cell_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cell_smem));
+      granted = cell_smem;
+    }
+  }
   if (sb + gcb > 0) cell_kernel<<<sb + gcb, 64, cell_smem, st>>>(a, sb);
   if (events) CUDA_TRY(cudaEventRecord(events[3], st));
   CUDA_TRY(cudaGetLastError());

@@ -587,7 +587,7 @@ int device_be_solve(_p_TDy *t, double dt, double *dU, const TDyNewtonOptions &o,
   SCUDA(cudaMemcpyAsync(s->x, dU, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
   SCUDA(cudaMemcpyAsync(s->xb, dU, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
   std::vector<double> f0(ns, 0.0), fn(ns, 0.0), g2(ns, 0.0), lam(ns, 1.0);
-  std::vector<int> act(ns, 1), its(ns, 0), trial(ns, 0), commit(ns, 0), step_conv(ns, 0);
+  std::vector<int> act(ns, 1), its(ns, 0), trial(ns, 0), commit(ns, 0), step_conv(ns, 0), failed(ns, 0);
   std::vector<double> y2(ns, 0.0), x2(ns, 0.0);
   long long lin_total = 0;
   // F and J at x (= xb for every instance after each evaluation below), and
@@ -609,6 +609,11 @@ int device_be_solve(_p_TDy *t, double dt, double *dU, const TDyNewtonOptions &o,
     bool any = false;
     for (int g = 0; g < ns; g++) {
       if (act[g]) {
+        if (!std::isfinite(fn[g]) || !std::isfinite(f0[g])) {  // diverged: stop, reported as not converged
+          act[g] = 0;
+          failed[g] = 1;
+          continue;
+        }
         const bool done = !(fn[g] > o.atol) || fn[g] <= o.rtol * f0[g];
         if (done || it == o.max_it) act[g] = 0;  // converged, or out of iterations (reported below)
         else its[g] = it + 1;
@@ -648,7 +653,12 @@ int device_be_solve(_p_TDy *t, double dt, double *dU, const TDyNewtonOptions &o,
         commit[g] = 0;
         if (!trial[g]) continue;
         const double f = fn[g] * fn[g], gg = g2[g];
-        if ((std::isfinite(gg) && gg <= (1.0 - 2.0 * alpha * lam[g]) * f) || ls == max_backtracks) {
+        if (!std::isfinite(gg) && ls == max_backtracks) {
+          // no finite trial point along the step: keep the last state, stop
+          trial[g] = 0;
+          act[g] = 0;
+          failed[g] = 1;
+        } else if ((std::isfinite(gg) && gg <= (1.0 - 2.0 * alpha * lam[g]) * f) || ls == max_backtracks) {
           commit[g] = 1;  // accepted (or the smallest step after the last backtrack)
           trial[g] = 0;
           fn[g] = std::sqrt(gg);
@@ -693,7 +703,7 @@ int device_be_solve(_p_TDy *t, double dt, double *dU, const TDyNewtonOptions &o,
   double worst = 0.0;
   for (int g = 0; g < ns; g++) {
     const double rel = f0[g] > 0.0 ? fn[g] / f0[g] : 0.0;
-    const bool ok = !(fn[g] > o.atol) || rel <= o.rtol || step_conv[g];
+    const bool ok = !failed[g] && std::isfinite(fn[g]) && (!(fn[g] > o.atol) || rel <= o.rtol || step_conv[g]);
     conv += ok ? 1 : 0;
     worst = std::max(worst, rel);
     maxit = std::max(maxit, its[g]);

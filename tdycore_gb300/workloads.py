@@ -290,3 +290,46 @@ def batched_columns(ninst=4096, seed_offset=0, cell=1.0, gap=1.0, top_excess=200
     t._props = {"K": K, "poro": poro, "m": m, "alpha": alpha}
     return t, U, info
 
+
+def infiltration_prisms(ntri=200_000, nlayers=40, lx=1000.0, ly=1000.0, seed_offset=0, top_flux=1e-7):
+    """Triangular prisms for the mixed-precision infiltration run: a seeded
+    Delaunay triangulation of uniform random points on an lx x ly square
+    (about ``ntri`` triangles), extruded into ``nlayers`` z-aligned layers of
+    thickness ~ U(0.1, 2) m; per cell a symmetric positive-definite K with
+    log10 eigenvalues ~ N(-12, 1) and a random rotation, porosity ~ U(0.05,
+    0.35), van Genuchten alpha ~ logU(1e-5, 1e-3) 1/Pa and m ~ U(0.2, 0.6),
+    Sr 0.15, constant density.  Start: hydrostatic (998 kg/m^3) with the water
+    table at half the depth, plus N(0, 10 Pa) noise.  Boundaries: no flow;
+    the infiltration (``top_flux`` m/s downward through the top surface) is a
+    source rho * q * A in each top cell.  Returns (tdy, U0, top_cells,
+    top_source, info)."""
+    rng = _rng(30 + seed_offset)
+    xy, tris = delaunay_surface(max(ntri // 2, 3), lx, ly, rng)
+    dz = rng.uniform(0.1, 2.0, nlayers)
+    levels = np.concatenate([[0.0], np.cumsum(dz)])
+    z = np.repeat(levels[:, None], xy.shape[0], axis=1)
+    t = create_richards_mpfao()
+    t.set_extruded_mesh(xy, tris, z)
+    t.set_from_options()
+    nt = tris.shape[0]
+    nc = nlayers * nt
+    t.set_permeability_values(random_spd(nc, _rng(31 + seed_offset)).reshape(nc, 9))
+    r = _rng(32 + seed_offset)
+    t.set_porosity_values(r.uniform(0.05, 0.35, nc))
+    m = r.uniform(0.2, 0.6, nc)
+    t.set_vangenuchten_values(m, 10.0 ** r.uniform(-5.0, -3.0, nc))
+    t.set_mualem_values(m)
+    t.set_constant_residual_saturation(0.15)
+    t.set_water_density_type(WATER_DENSITY_CONSTANT)
+    t.set_boundary_pressure_type_function(lambda x, y, zz: np.full(np.shape(x), NEUMANN_BC))
+    depth = levels[-1]
+    layer = np.arange(nc) // nt
+    zc = 0.5 * (levels[layer] + levels[layer + 1])
+    U = PREF + 998.0 * GRAVITY * (0.5 * depth - zc) + _rng(33 + seed_offset).normal(0.0, 10.0, nc)
+    a, b, c = xy[tris[:, 0]], xy[tris[:, 1]], xy[tris[:, 2]]
+    area = 0.5 * np.abs((b[:, 0] - a[:, 0]) * (c[:, 1] - a[:, 1]) - (b[:, 1] - a[:, 1]) * (c[:, 0] - a[:, 0]))
+    top = np.arange((nlayers - 1) * nt, nc, dtype=np.int32)
+    info = {"workload": f"infiltration_prisms_{nt}tri_{nlayers}layers", "ncells": nc, "seed": MASTER_SEED,
+            "top_flux_m_per_s": top_flux}
+    return t, U, top, 998.0 * top_flux * area, info
+

@@ -185,3 +185,30 @@ def test_device_built_trans_in_setup_view(name):
             continue
         scale = np.abs(Th[a:b]).max()
         assert np.all(np.abs(Td[a:b] - Th[a:b]) <= 1e-13 * scale), v
+
+
+def test_long_jacobian_rows_prisms():
+    """Delaunay prisms whose high-valence vertices give Jacobian rows of more
+    than 96 entries (the cell gather then stages its rows in more than 48 KB of
+    shared memory); parity with the oracle as for every other mesh."""
+    import tdycore_gb300 as T_
+    from tdycore_gb300.workloads import infiltration_prisms
+
+    T_.options_clear()
+    t, U, top, src, _ = infiltration_prisms(6000, 3)
+    t.setup()
+    rows = np.diff(t.rowptr)
+    assert rows.max() > 96, rows.max()
+    t.set_source_sink_values(src, cells=top)
+    o = Oracle(t.setup_view())
+    rng = np.random.default_rng(4)
+    U = U + rng.normal(0.0, 2e3, U.size)
+    Uprev = U + rng.normal(0.0, 50.0, U.size)
+    t.set_dtime(DT)
+    t.presolve(Uprev)
+    o.snes_presolve(Uprev, DT)
+    R, J = t.snes_function_jacobian(U)
+    Rr, Rm = o.snes_function(U, with_mag=True)
+    Jr, Jm = o.snes_jacobian(U, with_mag=True)
+    assert_close(R, Rr, Rm, R_TOL, "prisms SNES residual")
+    assert_close(J, Jr, Jm, J_TOL, "prisms SNES Jacobian")
