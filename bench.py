@@ -323,6 +323,154 @@ def batched_config4(ninst=4096, sample=64, dt=3600.0):
     }
 
 
+def prisms_config3(ntri=20000, nlayers=40, steps=20, dt=20.0, rotation="vertical", oracle_every_step_max_cells=4_000_000):
+    """Config 3: infiltration (1e-7 m/s through the top) into a dry soil on
+    Delaunay triangular prisms with per-cell full-tensor K, advanced ``steps``
+    backward-Euler steps of ``dt`` by the device Newton in the mixed form
+    (FP64 residual, FP32 Jacobian and inner solve).  Each step is also solved
+    from the same start in plain FP64 (FP64 Jacobian and inner solve), and the
+    FP64 oracle's residual of the mixed result relative to its residual at the
+    start of the step is reported per step (first and last step only above
+    ``oracle_every_step_max_cells``).
+
+    The step is short because MPFA-O on obtuse Delaunay triangles is not
+    monotone: where flux coefficients outweigh the accumulation term (which
+    scales with cell area / dt) the Jacobian has negative diagonal entries and
+    the line-preconditioned Krylov solve diverges.  Measured: 80 k cells
+    converge every step at dt = 600 s, 800 k cells at 20 s but not at 60 s."""
+    import torch
+
+    import tdycore_gb300 as T
+    from tdycore_gb300.workloads import infiltration_prisms
+    from oracle import Oracle
+
+    T.options_clear()
+    t0 = time.perf_counter()
+    t, U0, top, src, info = infiltration_prisms(ntri, nlayers, rotation=rotation)
+    t.setup()
+    t.set_source_sink_values(src, cells=top)
+    setup_s = time.perf_counter() - t0
+    nc, nnz = t.ncells, int(t.nnz)
+    log(f"config 3: {nc} cells, nnz {nnz}, setup {setup_s:.1f} s")
+    o = Oracle(t.setup_view())
+    dev = torch.device("cuda")
+    d = torch.tensor(U0, dtype=torch.float64, device=dev)
+    # warm-up: spmv autotune and graph capture of both arithmetic modes
+    for fp32 in (True, False):
+        w = d.clone()
+        t.backward_euler_step_device(w, dt, fp32=fp32)
+    del w
+    every = nc <= oracle_every_step_max_cells
+    per_step, mixed_s, fp64_s = [], 0.0, 0.0
+    for s in range(steps):
+        Un = d.clone()
+        d64 = d.clone()
+        torch.cuda.synchronize()
+        ts = time.perf_counter()
+        st, its, rel = t.backward_euler_step_device(d, dt, fp32=True)
+        torch.cuda.synchronize()
+        tm = time.perf_counter() - ts
+        ts = time.perf_counter()
+        st64, its64, rel64 = t.backward_euler_step_device(d64, dt, fp32=False)
+        torch.cuda.synchronize()
+        td = time.perf_counter() - ts
+        mixed_s += tm
+        fp64_s += td
+        diff = float(torch.max(torch.abs(d - d64) / torch.abs(d64)).item())
+        row = {"step": s + 1, "newton_mixed": int(its[0]), "newton_fp64": int(its64[0]),
+               "linear_mixed": st["linear_iterations"], "linear_fp64": st64["linear_iterations"],
+               "converged_mixed": st["converged"], "converged_fp64": st64["converged"],
+               "rel_residual_device": float(rel[0]), "mixed_s": tm, "fp64_s": td,
+               "max_rel_diff_mixed_vs_fp64": diff}
+        if every or s in (0, steps - 1):
+            un, u1 = Un.cpu().numpy(), d.cpu().numpy()
+            o.snes_presolve(un, dt)
+            f0 = np.linalg.norm(o.snes_function(un))
+            f1, m1 = o.snes_function(u1, with_mag=True)
+            row["oracle_rel_residual"] = float(np.linalg.norm(f1) / f0)
+            row["oracle_residual_over_scale"] = float(np.linalg.norm(f1) / np.linalg.norm(m1))
+        per_step.append(row)
+        log(f"config 3 step {s + 1}: {row}")
+    U = d.cpu().numpy()
+    t.destroy()
+    T.options_clear()
+    judged = [r for r in per_step if "oracle_rel_residual" in r]
+    return {
+        "workload": info["workload"], "ncells": nc, "nnz_jacobian": nnz,
+        "rotation": info["rotation"], "van_genuchten": info["van_genuchten"],
+        "initial_pressure_pa": info["initial_pressure_pa"], "depth_m": info["depth_m"],
+        "top_flux_m_per_s": info["top_flux_m_per_s"], "dt_s": dt, "steps": steps, "setup_s": setup_s,
+        "mixed_s_total": mixed_s, "fp64_s_total": fp64_s, "speedup_mixed_vs_fp64": fp64_s / mixed_s,
+        "all_converged_mixed": all(r["converged_mixed"] == 1 for r in per_step),
+        "max_oracle_rel_residual": max(r["oracle_rel_residual"] for r in judged),
+        "max_rel_diff_mixed_vs_fp64": max(r["max_rel_diff_mixed_vs_fp64"] for r in per_step),
+        "pressure_range_pa_final": [float(U.min()), float(U.max())],
+        "per_step": per_step,
+        "note": "mixed = FP64 residual with FP32 Jacobian and inner solve; fp64 = the same step from the same "
+                "start with FP64 Jacobian and inner solve; oracle_rel_residual = ||F(U_mixed)|| / ||F(U_n)|| "
+                "from the FP64 CPU oracle",
+    }
+
+
+def prisms_eval_full_size(ntri=200_000, nlayers=40, reps=10, dt=3600.0):
+    """Config 3 at its full size and tensor field (Delaunay prisms, per-cell
+    K with a uniform random 3-D rotation): one mixed-form evaluation (FP64
+    residual, Jacobian rounded to FP32 for the inner solve) against the FP64
+    oracle, and the device F+J time, at a state with saturated and
+    unsaturated cells."""
+    import torch
+
+    import tdycore_gb300 as T
+    from tdycore_gb300.workloads import infiltration_prisms
+    from oracle import Oracle
+
+    T.options_clear()
+    t0 = time.perf_counter()
+    t, U0, top, src, info = infiltration_prisms(ntri, nlayers, rotation="full")
+    t.setup()
+    t.set_source_sink_values(src, cells=top)
+    setup_s = time.perf_counter() - t0
+    nc, nnz = t.ncells, int(t.nnz)
+    rng = np.random.default_rng(5)
+    U = U0 + 2.0e4 + rng.normal(0.0, 2.0e3, nc)
+    Uprev = U + rng.normal(0.0, 50.0, nc)
+    dev = torch.device("cuda")
+    dU = torch.tensor(U, dtype=torch.float64, device=dev)
+    dUp = torch.tensor(Uprev, dtype=torch.float64, device=dev)
+    dR = torch.empty(nc, dtype=torch.float64, device=dev)
+    dJ = torch.empty(nnz, dtype=torch.float64, device=dev)
+    st = torch.cuda.current_stream()  # the launches and the events on one stream
+    t.set_dtime(dt)
+    t.presolve_device(dUp, stream=st.cuda_stream)
+    for _ in range(3):
+        t.snes_function_jacobian_device(dU, dR, dJ, stream=st.cuda_stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(st)
+    for _ in range(reps):
+        t.snes_function_jacobian_device(dU, dR, dJ, stream=st.cuda_stream)
+    e1.record(st)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    R, J, J32 = dR.cpu().numpy(), dJ.cpu().numpy(), dJ.float().cpu().numpy().astype(np.float64)
+    o = Oracle(t.setup_view())
+    o.snes_presolve(Uprev, dt)
+    Rr, Rm = o.snes_function(U, with_mag=True)
+    Jr, Jm = o.snes_jacobian(U, with_mag=True)
+    tiny = np.finfo(float).tiny
+    nzj = np.abs(Jr) > 0
+    t.destroy()
+    T.options_clear()
+    return {"workload": info["workload"], "ncells": nc, "nnz_jacobian": nnz, "rotation": "full",
+            "setup_s": setup_s, "fj_ms": ms, "fj_cells_per_s": nc / (ms * 1e-3),
+            "R_err_over_scale": float(np.max(np.abs(R - Rr) / np.maximum(Rm, tiny))),
+            "J_fp64_err_over_scale": float(np.max(np.abs(J - Jr) / np.maximum(Jm, tiny))),
+            "J_fp32_err_over_scale": float(np.max(np.abs(J32 - Jr) / np.maximum(Jm, tiny))),
+            "J_fp32_max_rel_err": float(np.max(np.abs(J32[nzj] - Jr[nzj]) / np.abs(Jr[nzj]))),
+            "note": "state: uniform Pref plus N(0, 2 kPa) (saturated and unsaturated cells), previous state "
+                    "N(0, 50 Pa) from it; errors in units of the oracle's per-entry error scale"}
+
+
 def serving_config5(nreq=160, rate=80.0, slots=32):
     """Config 5: Poisson arrivals of column/subdomain requests (5 % of them
     64 x 64 x 50 cells), 24 hourly backward-Euler steps each with top-flux
@@ -556,6 +704,18 @@ def run_gpu(args, rank, world, local_rank):
                 cfg5 = serving_config5(args.serve_requests)
             except Exception as e:
                 cfg5 = {"error": repr(e)}
+        cfg3 = None
+        if args.prisms_triangles > 0:
+            try:
+                cfg3 = prisms_config3(args.prisms_triangles, dt=args.prisms_dt)
+            except Exception as e:
+                cfg3 = {"error": repr(e)}
+        if args.prisms_eval_triangles > 0:
+            try:
+                ev = prisms_eval_full_size(args.prisms_eval_triangles)
+            except Exception as e:
+                ev = {"error": repr(e)}
+            cfg3 = dict(cfg3 or {}, mixed_form_evaluation=ev)
         cfg4 = None
         if args.batch_instances > 0:
             try:
@@ -588,6 +748,7 @@ def run_gpu(args, rank, world, local_rank):
             "gpu_launches": args.steps * launches,
             "parity_full_size": parity,
             "config1_newton": cfg1,
+            "config3_prisms_mixed_precision": cfg3,
             "config4_batched": cfg4,
             "config5_serving": cfg5,
             "setup_s": {"trans_on_host": info["setup_s"],
@@ -619,6 +780,13 @@ def main():
                     help="arithmetic of the Jacobian products at interior hexahedral vertices")
     ap.add_argument("--serve-requests", type=int, default=160,
                     help="requests of the serving measurement (0 skips it)")
+    ap.add_argument("--prisms-triangles", type=int, default=20000,
+                    help="surface triangles of the prism infiltration measurement (0 skips it)")
+    ap.add_argument("--prisms-dt", type=float, default=20.0,
+                    help="time step of the prism infiltration measurement (s)")
+    ap.add_argument("--prisms-eval-triangles", type=int, default=0,
+                    help="surface triangles of the mixed-form F+J evaluation on prisms with 3-D rotated K "
+                         "(200000 is the full configuration; 0 skips it)")
     ap.add_argument("--batch-instances", type=int, default=4096,
                     help="instances of the batched-solve measurement (0 skips it)")
     ap.add_argument("--profile", action="store_true",

@@ -653,15 +653,16 @@ int device_be_solve(_p_TDy *t, double dt, double *dU, const TDyNewtonOptions &o,
         commit[g] = 0;
         if (!trial[g]) continue;
         const double f = fn[g] * fn[g], gg = g2[g];
-        if (!std::isfinite(gg) && ls == max_backtracks) {
-          // no finite trial point along the step: keep the last state, stop
+        if (std::isfinite(gg) && (gg <= (1.0 - 2.0 * alpha * lam[g]) * f || (ls == max_backtracks && gg < f))) {
+          commit[g] = 1;  // sufficient decrease (or, at the smallest step, any decrease)
+          trial[g] = 0;
+          fn[g] = std::sqrt(gg);
+        } else if (ls == max_backtracks) {
+          // line search failure (PETSc's DIVERGED_LINE_SEARCH): the smallest
+          // step does not lower ||F|| either; keep the last accepted state, stop
           trial[g] = 0;
           act[g] = 0;
           failed[g] = 1;
-        } else if ((std::isfinite(gg) && gg <= (1.0 - 2.0 * alpha * lam[g]) * f) || ls == max_backtracks) {
-          commit[g] = 1;  // accepted (or the smallest step after the last backtrack)
-          trial[g] = 0;
-          fn[g] = std::sqrt(gg);
         } else {
           const double slope = -f;
           double lt = std::isfinite(gg) ? -slope * lam[g] * lam[g] / (gg - f - 2.0 * slope * lam[g]) : 0.0;
@@ -675,7 +676,8 @@ int device_be_solve(_p_TDy *t, double dt, double *dU, const TDyNewtonOptions &o,
       SCUDA(cudaGetLastError());
       if (!pending) break;
     }
-    // every instance now has x == xb, so F and J hold the accepted states.
+    // every instance still active now has x == xb, so its F and J rows hold
+    // the accepted state (instances do not couple).
     // Step test (SNESConvergedDefault): ||y|| < stol ||x|| per instance, with
     // y the full Newton step (PETSc's backtracking line search reports the
     // norm of the step before its lambda scaling), so a step cut short by the

@@ -161,11 +161,24 @@ def spe10_like(nx=60, ny=220, nz=85, lx=365.76, ly=670.56, lz=51.816, jitter=0.1
 
 
 def delaunay_surface(npts, lx, ly, rng):
+    """Delaunay triangulation (counter-clockwise triangles) of ``npts``
+    uniform random points in [0, lx] x [0, ly] plus points along the four
+    sides at the mean interior spacing h (corners included); random points
+    closer than h/4 to a side are dropped.  Without the side points every
+    side is one hull edge, and interior points close to it form triangles
+    with angles near 180 degrees, on which MPFA-O is far from monotone
+    (negative Jacobian diagonals, indefinite linear systems)."""
     from scipy.spatial import Delaunay
 
     pts = rng.uniform(0.0, 1.0, (npts, 2)) * [lx, ly]
-    corners = np.array([[0, 0], [lx, 0], [lx, ly], [0, ly]], dtype=float)
-    pts = np.vstack([corners, pts])
+    h = np.sqrt(lx * ly / max(npts, 1))
+    margin = np.minimum(np.minimum(pts[:, 0], lx - pts[:, 0]), np.minimum(pts[:, 1], ly - pts[:, 1]))
+    pts = pts[margin >= 0.25 * h]
+    nx, ny = max(int(round(lx / h)), 1), max(int(round(ly / h)), 1)
+    sx, sy = np.linspace(0.0, lx, nx + 1), np.linspace(0.0, ly, ny + 1)
+    side = np.vstack([np.c_[sx, np.zeros_like(sx)], np.c_[sx, np.full_like(sx, ly)],
+                      np.c_[np.zeros(ny - 1), sy[1:-1]], np.c_[np.full(ny - 1, lx), sy[1:-1]]])
+    pts = np.vstack([side, pts])
     tri = Delaunay(pts)
     simp = tri.simplices.astype(np.int32)
     # counter-clockwise orientation
@@ -173,15 +186,37 @@ def delaunay_surface(npts, lx, ly, rng):
     cross = (b[:, 0] - a[:, 0]) * (c[:, 1] - a[:, 1]) - (b[:, 1] - a[:, 1]) * (c[:, 0] - a[:, 0])
     flip = cross < 0
     simp[flip] = simp[flip][:, [0, 2, 1]]
-    # drop slivers on the hull (area ~ 0)
+    # drop degenerate triangles (collinear side points)
     area = 0.5 * np.abs(cross)
     keep = area > 1e-9 * lx * ly / max(len(simp), 1)
     return pts, simp[keep]
 
 
-def random_spd(nc, rng, mean=-12.0, std=1.0):
-    eig = 10.0 ** (mean + std * rng.standard_normal((nc, 3)))
-    q, _ = np.linalg.qr(rng.standard_normal((nc, 3, 3)))
+def random_spd(nc, rng, mean=-12.0, std=1.0, rotation="full", anisotropy_std=None):
+    """Per-cell symmetric positive-definite K with log10 eigenvalues ~ N(mean,
+    std) and a random rotation: a uniform random 3-D rotation ("full") or a
+    rotation by a uniform angle about the vertical axis ("vertical", which
+    leaves K_xz = K_yz = 0 and the horizontal 2x2 block full).  With
+    ``anisotropy_std`` s the three log10 eigenvalues of a cell share a common
+    N(0, std^2 - s^2) part and differ by independent N(0, s^2) parts (each
+    eigenvalue still ~ N(mean, std^2); log10 of the anisotropy ratio then has
+    standard deviation s * sqrt(2) instead of std * sqrt(2))."""
+    if anisotropy_std is None:
+        eig = 10.0 ** (mean + std * rng.standard_normal((nc, 3)))
+    else:
+        if not 0.0 <= anisotropy_std <= std:
+            raise ValueError("anisotropy_std must lie in [0, std]")
+        common = np.sqrt(std * std - anisotropy_std * anisotropy_std) * rng.standard_normal((nc, 1))
+        eig = 10.0 ** (mean + common + anisotropy_std * rng.standard_normal((nc, 3)))
+    if rotation == "full":
+        q, _ = np.linalg.qr(rng.standard_normal((nc, 3, 3)))
+    elif rotation == "vertical":
+        th = rng.uniform(0.0, 2.0 * np.pi, nc)
+        c, s = np.cos(th), np.sin(th)
+        q = np.zeros((nc, 3, 3))
+        q[:, 0, 0], q[:, 0, 1], q[:, 1, 0], q[:, 1, 1], q[:, 2, 2] = c, -s, s, c, 1.0
+    else:
+        raise ValueError(f"rotation must be 'full' or 'vertical', not {rotation!r}")
     K = np.einsum("nij,nj,nkj->nik", q, eig, q)
     return 0.5 * (K + np.transpose(K, (0, 2, 1)))
 
@@ -291,18 +326,35 @@ def batched_columns(ninst=4096, seed_offset=0, cell=1.0, gap=1.0, top_excess=200
     return t, U, info
 
 
-def infiltration_prisms(ntri=200_000, nlayers=40, lx=1000.0, ly=1000.0, seed_offset=0, top_flux=1e-7):
-    """Triangular prisms for the mixed-precision infiltration run: a seeded
-    Delaunay triangulation of uniform random points on an lx x ly square
-    (about ``ntri`` triangles), extruded into ``nlayers`` z-aligned layers of
-    thickness ~ U(0.1, 2) m; per cell a symmetric positive-definite K with
-    log10 eigenvalues ~ N(-12, 1) and a random rotation, porosity ~ U(0.05,
-    0.35), van Genuchten alpha ~ logU(1e-5, 1e-3) 1/Pa and m ~ U(0.2, 0.6),
-    Sr 0.15, constant density.  Start: hydrostatic (998 kg/m^3) with the water
-    table at half the depth, plus N(0, 10 Pa) noise.  Boundaries: no flow;
-    the infiltration (``top_flux`` m/s downward through the top surface) is a
-    source rho * q * A in each top cell.  Returns (tdy, U0, top_cells,
-    top_source, info)."""
+def infiltration_prisms(ntri=200_000, nlayers=40, lx=1000.0, ly=1000.0, seed_offset=0, top_flux=1e-7,
+                        rotation="vertical", suction=2.0e4, vg_alpha=1.0e-4, vg_m=0.5, anisotropy_std=None):
+    """Infiltration into a dry soil on triangular prisms: a seeded Delaunay
+    triangulation of uniform random points on an lx x ly square (about
+    ``ntri`` triangles), extruded into ``nlayers`` z-aligned layers of
+    thickness ~ U(0.1, 2) m.  Per cell a symmetric positive-definite K with
+    log10 eigenvalues ~ N(-12, 1) and a random rotation (``rotation``, see
+    random_spd) and porosity ~ U(0.05, 0.35); one van Genuchten/Mualem soil
+    (``vg_alpha`` 1/Pa, ``vg_m``), Sr 0.15, constant density.  Start: uniform
+    pressure Pref - ``suction``.  Boundaries: no flow; the infiltration
+    (``top_flux`` m/s downward through the top surface) is a source
+    rho * q * A in each top cell.
+
+    Why these choices (measured with the oracle and an exact or Krylov linear
+    solve on 5 k - 8 M cells):
+    * rotations about the vertical axis: with a random 3-D rotation the
+      two-point gravity term of the reference (src/fv/mpfao/tdympfao.c:
+      2145-2265, A (n . K u) (g . u) with u the centroid-to-centroid
+      direction, zero on the vertical faces of z-aligned prisms) cannot
+      balance the MPFA-O pressure flux n . K grad(p) that K_xz and K_yz carry
+      on those faces; no hydrostatic or uniform start is near the discrete
+      equilibrium and Newton stalls at 1e-2 to 1e-3 relative residual;
+    * one soil: with van Genuchten parameters that differ between neighbours
+      (per cell or per layer), upwinded kr jumps wherever a flux passes
+      through zero, the residual has first-order kinks there and Newton's
+      line search stalls at 1e-4 to 1e-2; with one soil the jump is of second
+      order and Newton converges quadratically (3-6 iterations per step).
+
+    Returns (tdy, U0, top_cells, top_source, info)."""
     rng = _rng(30 + seed_offset)
     xy, tris = delaunay_surface(max(ntri // 2, 3), lx, ly, rng)
     dz = rng.uniform(0.1, 2.0, nlayers)
@@ -313,23 +365,22 @@ def infiltration_prisms(ntri=200_000, nlayers=40, lx=1000.0, ly=1000.0, seed_off
     t.set_from_options()
     nt = tris.shape[0]
     nc = nlayers * nt
-    t.set_permeability_values(random_spd(nc, _rng(31 + seed_offset)).reshape(nc, 9))
+    K = random_spd(nc, _rng(31 + seed_offset), rotation=rotation, anisotropy_std=anisotropy_std)
+    t.set_permeability_values(K.reshape(nc, 9))
     r = _rng(32 + seed_offset)
     t.set_porosity_values(r.uniform(0.05, 0.35, nc))
-    m = r.uniform(0.2, 0.6, nc)
-    t.set_vangenuchten_values(m, 10.0 ** r.uniform(-5.0, -3.0, nc))
+    m = np.full(nc, vg_m)
+    t.set_vangenuchten_values(m, np.full(nc, vg_alpha))
     t.set_mualem_values(m)
     t.set_constant_residual_saturation(0.15)
     t.set_water_density_type(WATER_DENSITY_CONSTANT)
     t.set_boundary_pressure_type_function(lambda x, y, zz: np.full(np.shape(x), NEUMANN_BC))
-    depth = levels[-1]
-    layer = np.arange(nc) // nt
-    zc = 0.5 * (levels[layer] + levels[layer + 1])
-    U = PREF + 998.0 * GRAVITY * (0.5 * depth - zc) + _rng(33 + seed_offset).normal(0.0, 10.0, nc)
+    U = np.full(nc, PREF - suction)
     a, b, c = xy[tris[:, 0]], xy[tris[:, 1]], xy[tris[:, 2]]
     area = 0.5 * np.abs((b[:, 0] - a[:, 0]) * (c[:, 1] - a[:, 1]) - (b[:, 1] - a[:, 1]) * (c[:, 0] - a[:, 0]))
     top = np.arange((nlayers - 1) * nt, nc, dtype=np.int32)
     info = {"workload": f"infiltration_prisms_{nt}tri_{nlayers}layers", "ncells": nc, "seed": MASTER_SEED,
-            "top_flux_m_per_s": top_flux}
+            "top_flux_m_per_s": top_flux, "rotation": rotation, "initial_pressure_pa": PREF - suction,
+            "van_genuchten": {"alpha_per_pa": vg_alpha, "m": vg_m}, "depth_m": float(levels[-1])}
     return t, U, top, 998.0 * top_flux * area, info
 

@@ -187,22 +187,51 @@ def test_device_built_trans_in_setup_view(name):
         assert np.all(np.abs(Td[a:b] - Th[a:b]) <= 1e-13 * scale), v
 
 
+def hub_prisms(nring=42, nlayers=3):
+    """Prisms over the Delaunay triangulation of three close hub points inside
+    a ring of ``nring`` points: each hub has valence ~17 (within the vertex
+    kernel's limits of 64 rows and 64 cells per vertex), and a wedge touching
+    the hubs shares a vertex with ~46 triangles' wedges in each of three
+    layers, so its Jacobian row has more than 96 entries."""
+    import tdycore_gb300 as T_
+    from scipy.spatial import Delaunay
+    from tdycore_gb300 import workloads as W
+
+    ang = np.linspace(0.0, 2.0 * np.pi, nring, endpoint=False)
+    hub = np.linspace(0.0, 2.0 * np.pi, 3, endpoint=False) + 0.3
+    xy = np.vstack([np.c_[2.0 * np.cos(hub), 2.0 * np.sin(hub)], np.c_[20.0 * np.cos(ang), 20.0 * np.sin(ang)]])
+    tris = Delaunay(xy).simplices.astype(np.int32)
+    P = xy[tris]
+    cw = (P[:, 1, 0] - P[:, 0, 0]) * (P[:, 2, 1] - P[:, 0, 1]) - (P[:, 1, 1] - P[:, 0, 1]) * (P[:, 2, 0] - P[:, 0, 0]) < 0
+    tris[cw] = tris[cw][:, [0, 2, 1]]
+    z = np.repeat(np.array([0.0, 0.7, 2.0, 3.1])[:nlayers + 1, None], xy.shape[0], axis=1)
+    nc = nlayers * tris.shape[0]
+    rng = np.random.default_rng(41)
+    T_.options_clear()
+    t = T_.create_richards_mpfao()
+    t.set_extruded_mesh(xy, tris, z)
+    t.set_from_options()
+    t.set_permeability_values(W.random_spd(nc, rng).reshape(nc, 9))
+    t.set_porosity_values(rng.uniform(0.05, 0.35, nc))
+    m = rng.uniform(0.2, 0.6, nc)
+    t.set_vangenuchten_values(m, 10.0 ** rng.uniform(-5.0, -3.0, nc))
+    t.set_mualem_values(m)
+    t.set_constant_residual_saturation(0.15)
+    t.set_water_density_type(T_.WATER_DENSITY_CONSTANT)
+    t.set_boundary_pressure_type_function(lambda x, y, zz: np.full(np.shape(x), T_.NEUMANN_BC))
+    U = 101325.0 + rng.normal(0.0, 2e3, nc)
+    return t, U, rng
+
+
 def test_long_jacobian_rows_prisms():
-    """Delaunay prisms whose high-valence vertices give Jacobian rows of more
+    """Prisms around three high-valence vertices give Jacobian rows of more
     than 96 entries (the cell gather then stages its rows in more than 48 KB of
     shared memory); parity with the oracle as for every other mesh."""
-    import tdycore_gb300 as T_
-    from tdycore_gb300.workloads import infiltration_prisms
-
-    T_.options_clear()
-    t, U, top, src, _ = infiltration_prisms(6000, 3)
+    t, U, rng = hub_prisms()
     t.setup()
     rows = np.diff(t.rowptr)
     assert rows.max() > 96, rows.max()
-    t.set_source_sink_values(src, cells=top)
     o = Oracle(t.setup_view())
-    rng = np.random.default_rng(4)
-    U = U + rng.normal(0.0, 2e3, U.size)
     Uprev = U + rng.normal(0.0, 50.0, U.size)
     t.set_dtime(DT)
     t.presolve(Uprev)
