@@ -439,7 +439,7 @@ def prisms_eval_full_size(ntri=200_000, nlayers=40, reps=10, dt=3600.0):
     dUp = torch.tensor(Uprev, dtype=torch.float64, device=dev)
     dR = torch.empty(nc, dtype=torch.float64, device=dev)
     dJ = torch.empty(nnz, dtype=torch.float64, device=dev)
-    st = torch.cuda.current_stream()  # the launches and the events on one stream
+    st = torch.cuda.Stream(device=dev)  # the launches and the events on one (non-null) stream
     t.set_dtime(dt)
     t.presolve_device(dUp, stream=st.cuda_stream)
     for _ in range(3):

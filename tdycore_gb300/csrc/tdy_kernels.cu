@@ -49,9 +49,8 @@ namespace tdy {
 
 #define TDY_MAX_ROWS 64
 #define TDY_MAX_NINT 64
-// Jacobian row length: the gather program stores slots in 8 bits; the
-// generic cell kernel stages 64 rows of this length in shared memory
-// (255 doubles x 64 = 130 KB, within the 227 KB a block may use)
+// Jacobian row length: the gather program stores slots in 8 bits (the
+// generic cell kernel stages one row per warp in shared memory)
 #define TDY_MAX_ROW_NNZ 255
 
 struct DevArgs {
@@ -85,6 +84,7 @@ struct DevArgs {
   const int *cellc, *facec;
   // generic vertices
   int ngen;
+  int gen_warp_doubles;  // shared memory of one generic-vertex warp (doubles)
   const int *gen_vertex;
   const int *v_row_off, *v_col_off, *v_nint;
   const long long *v_trans_off, *v_jv_off;
@@ -102,6 +102,7 @@ struct DevArgs {
   double *R, *J;
 };
 
+// timer groups: the state kernel, the vertex kernels, the cell kernels
 static const char *const kKernelNames[3] = {"state_kernel", "vertex_kernel", "cell_kernel"};
 
 struct DeviceState {
@@ -588,8 +589,14 @@ __device__ __forceinline__ void canon_vertex(const DevArgs &a, int block) {
 }
 
 // ---------------------------------------------------------------------------
-// 3. other vertices: per-vertex blocks
-__device__ __forceinline__ void generic_vertex(const DevArgs &a, int block) {
+// 3. other vertices.  Both forms below sum every Jacobian entry (c, b) of a
+// vertex block over the rows whose faces touch local cell c in row order,
+// each row's T term before its upwind-derivative terms, so they give the
+// same bits.
+//
+// (a) one thread per vertex, for meshes that are mostly canonical hexahedra
+// (their other vertices are few and small, and share the canonical launch)
+__device__ __forceinline__ void generic_vertex_thread(const DevArgs &a, int block) {
   const int g = block * blockDim.x + threadIdx.x;
   if (g >= a.ngen) return;
   const int v = a.gen_vertex[g];
@@ -656,15 +663,123 @@ __device__ __forceinline__ void generic_vertex(const DevArgs &a, int block) {
   }
 }
 
-// The other (heavier, per-vertex-block) vertices take the first blocks of the
-// launch so they overlap the canonical ones instead of trailing them.
+// (b) one warp per vertex, for meshes without canonical vertices.  Lanes
+// take the rows for the transmissibility products and upwinding, then the
+// entries of the block; the rows of each local cell come from a list built
+// in shared memory, so the lanes of an entry pass stay in step.
+constexpr int kGenWarps = 4;     // warps (vertices) per 128-thread block
+constexpr int kGenCellRows = 8;  // rows per local cell in the list; more take the scan
+
+__device__ __forceinline__ void generic_vertex_warp(const DevArgs &a, int block) {
+  extern __shared__ double gsh[];  // [kGenWarps][gen_warp_doubles]
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int g = block * kGenWarps + warp;
+  if (g >= a.ngen) return;  // whole warp
+  const int v = a.gen_vertex[g];
+  const int nint = a.v_nint[v];
+  const int r0 = a.v_row_off[v], nrow = a.v_row_off[v + 1] - r0;
+  const int c0 = a.v_col_off[v], ncol = a.v_col_off[v + 1] - c0;
+  const double *T = a.trans + a.v_trans_off[v];
+  double *Jv = a.scratch + a.v_jv_off[v];
+  double *Rv = Jv + nint * nint;
+  double *w = gsh + (size_t)warp * a.gen_warp_doubles;
+  double *Eu = w + TDY_MAX_ROWS, *Ed = Eu + TDY_MAX_ROWS, *fl = Ed + TDY_MAX_ROWS;
+  int *lup = reinterpret_cast<int *>(fl + TDY_MAX_ROWS), *ldn = lup + TDY_MAX_ROWS;
+  unsigned char *cnt = reinterpret_cast<unsigned char *>(ldn + TDY_MAX_ROWS);  // [TDY_MAX_NINT]
+  unsigned char *lst = cnt + TDY_MAX_NINT;                                    // [TDY_MAX_NINT][kGenCellRows]
+
+  for (int r = lane; r < nrow; r += 32) {
+    const double *Tr = T + (size_t)r * ncol;
+    double TP = 0.0;
+    for (int c = 0; c < ncol; c++) TP = __fma_rn(Tr[c], a.P[a.col_ext[c0 + c]], TP);
+    const int f = a.row_face[r0 + r];
+    const int up = a.f_up[f], dn = a.f_dn[f];
+    const double G = a.G[f];
+    const double den = __dadd_rn(a.hr[up], a.hr[dn]);
+    const double q = __fma_rn(den, G, TP);
+    const bool flowdn = q < 0.0;
+    const int u = flowdn ? up : dn;
+    const double lm = a.lam[u];
+    const bool zero = a.seep[u] != 0;
+    const double wr = zero ? 0.0 : __dmul_rn(den, lm);
+    fl[r] = -__dmul_rn(wr, q);
+    w[r] = wr;
+    if (zero) {
+      Eu[r] = 0.0;
+      Ed[r] = 0.0;
+    } else {
+      const double dlu = flowdn ? a.dlam[up] : 0.0, dld = flowdn ? 0.0 : a.dlam[dn];
+      const double g2 = q + den * G;
+      Eu[r] = a.hdr[up] * lm * g2 + den * dlu * q;
+      Ed[r] = a.hdr[dn] * lm * g2 + den * dld * q;
+    }
+    lup[r] = a.row_lup[r0 + r];
+    ldn[r] = a.row_ldn[r0 + r];
+  }
+  __syncwarp();
+  // rows of each local cell, in row order (count 255: more than the list holds)
+  for (int c = lane; c < nint; c += 32) {
+    int k = 0;
+    for (int r = 0; r < nrow; r++)
+      if (lup[r] == c || ldn[r] == c) {
+        if (k < kGenCellRows) lst[c * kGenCellRows + k] = (unsigned char)r;
+        k++;
+      }
+    cnt[c] = (unsigned char)(k <= kGenCellRows ? k : 255);
+  }
+  __syncwarp();
+  // The FP64 pipe is the bound here (a warp-wide FP64 instruction costs as
+  // many issue slots as it has lanes, active or not): walk only each cell's
+  // own rows, and pick signs and upwind terms by integer selects.
+  if (a.needR) {
+    for (int c = lane; c < nint; c += 32) {
+      const int kc = cnt[c];
+      const int kn = kc == 255 ? nrow : kc;
+      double s = 0.0;
+      for (int k = 0; k < kn; k++) {
+        const int r = kc == 255 ? k : lst[c * kGenCellRows + k];
+        if (lup[r] == c) s += fl[r];
+        if (ldn[r] == c) s -= fl[r];
+      }
+      Rv[c] = s;
+    }
+  }
+  if (!a.needJ) return;
+  const int nn = nint * nint;
+  for (int e = lane; e < nn; e += 32) {
+    const int c = e / nint, b = e - c * nint;
+    const int kc = cnt[c];
+    const int kn = kc == 255 ? nrow : kc;
+    double J = 0.0;
+    for (int k = 0; k < kn; k++) {
+      const int r = kc == 255 ? k : lst[c * kGenCellRows + k];
+      const int lu = lup[r], ld = ldn[r];
+      if (lu != c && ld != c) continue;  // only in the scan
+      const bool isup = lu == c;
+      const double wr = w[r], eu = Eu[r], ed = Ed[r];
+      J = fma(isup ? -wr : wr, T[(size_t)r * ncol + b], J);
+      // at most one of b == lu, b == ld holds
+      const double et = (b == lu) ? eu : ((b == ld) ? ed : 0.0);
+      J += isup ? -et : et;
+    }
+    Jv[e] = J;
+  }
+}
+
+// Canonical vertices (one thread each, register-heavy) share their launch
+// with the thread form of the other vertices, which take the first blocks so
+// they overlap the canonical ones; meshes without canonical vertices launch
+// the warp form on its own (a light kernel with high occupancy for its
+// latency-bound gathers).
 template <bool CONST_RHO, bool FFJ>
 __global__ void __launch_bounds__(128) vertex_kernel(DevArgs a, int gen_blocks) {
   if ((int)blockIdx.x >= gen_blocks)
     canon_vertex<CONST_RHO, FFJ>(a, blockIdx.x - gen_blocks);
   else
-    generic_vertex(a, blockIdx.x);
+    generic_vertex_thread(a, blockIdx.x);
 }
+
+__global__ void __launch_bounds__(128) generic_vertex_kernel(DevArgs a) { generic_vertex_warp(a, blockIdx.x); }
 
 // ---------------------------------------------------------------------------
 // 4. per-cell deterministic gather into R and the CSR row.
@@ -735,7 +850,8 @@ __device__ __forceinline__ void struct_cell(const DevArgs &a, int block) {
   }
 }
 
-__device__ __forceinline__ void generic_cell(const DevArgs &a, int block) {
+// Other cells, thread form (meshes with structured cells).
+__device__ __forceinline__ void generic_cell_thread(const DevArgs &a, int block) {
   extern __shared__ double rowbuf[];  // [warps][32 * max_row_nnz]
   const int gidx = block * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -773,12 +889,54 @@ __device__ __forceinline__ void generic_cell(const DevArgs &a, int block) {
   }
 }
 
+// Other cells, warp form (meshes without structured cells): one warp per
+// cell.  The row is staged in shared memory; the lanes take the columns of
+// each vertex block (distinct columns land in distinct slots) and the
+// vertices are added in the cell's corner order, as in the thread form.
+constexpr int kCellWarps = 4;  // warps (cells) per generic-cell block
+
+__device__ __forceinline__ void generic_cell_warp(const DevArgs &a, int block) {
+  extern __shared__ double rowbuf[];  // [kCellWarps][max_row_nnz]
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int gidx = block * kCellWarps + warp;
+  if (gidx >= a.ngc) return;  // whole warp
+  const int i = a.gc_cells[gidx];
+  const int k0 = a.cv_off[i], k1 = a.cv_off[i + 1];
+  if (a.needR && lane == 0) {
+    double s = 0.0;
+    for (int k = k0; k < k1; k++) s += a.scratch[a.cv_rbase[k]];
+    s += a.acc_a[i];
+    s -= a.acc_b[i];
+    a.R[i] = s;
+  }
+  if (!a.needJ) return;
+  double *row = rowbuf + (size_t)warp * a.max_row_nnz;
+  const int p0 = a.rowptr[i], rn = a.rowptr[i + 1] - p0;
+  for (int j = lane; j < rn; j += 32) row[j] = 0.0;
+  __syncwarp();
+  int diag = -1;
+  for (int k = k0; k < k1; k++) {
+    const int nint = a.cv_nint[k], stride = a.cv_stride[k];
+    const double *blk = a.scratch + a.cv_jbase[k];
+    const unsigned char *sl = a.cv_slots + a.cv_slot_off[k];
+    for (int b = lane; b < nint; b += 32) row[sl[b]] += blk[(long long)b * stride];
+    diag = sl[a.cv_local[k]];
+    __syncwarp();
+  }
+  if (lane == 0 && diag >= 0) row[diag] += a.jdiag[i];
+  __syncwarp();
+  double *out = a.J + p0;
+  for (int j = lane; j < rn; j += 32) out[j] = row[j];
+}
+
 __global__ void __launch_bounds__(64) cell_kernel(DevArgs a, int struct_blocks) {
   if ((int)blockIdx.x < struct_blocks)
     struct_cell(a, blockIdx.x);
   else
-    generic_cell(a, blockIdx.x - struct_blocks);
+    generic_cell_thread(a, blockIdx.x - struct_blocks);
 }
+
+__global__ void __launch_bounds__(32 * kCellWarps) generic_cell_kernel(DevArgs a) { generic_cell_warp(a, blockIdx.x); }
 
 // ---------------------------------------------------------------------------
 // Host side
@@ -876,6 +1034,9 @@ int device_setup(_p_TDy *t) {
   if (t->opt.setup_on_device && (ierr = device_canon_trans(t, a.cellc, a.facec, const_cast<double *>(a.Tc))))
     return ierr;
   a.ngen = (int)s.gen_vertex.size();
+  // per row: w, E_up, E_dn, flux (doubles) and the two local-cell indices
+  // (ints); per local cell: a row count and a list of kGenCellRows rows (bytes)
+  a.gen_warp_doubles = 5 * TDY_MAX_ROWS + (TDY_MAX_NINT * (1 + kGenCellRows) + 7) / 8;
   UP(a.gen_vertex, s.gen_vertex);
   UP(a.v_row_off, s.v_row_off);
   UP(a.v_col_off, s.v_col_off);
@@ -988,37 +1149,55 @@ int device_presolve_host(_p_TDy *t, const double *Uprev) {
 // The four launches of one evaluation; events[] (5 entries, or null) bracket
 // them for the per-kernel timers.
 static int launch_eval(const DevArgs &a, cudaStream_t st, cudaEvent_t *events) {
-  const size_t canon_smem = 36 * 128 * sizeof(double);
-  const size_t cell_smem = 64 * (size_t)(a.max_row_nnz > 27 ? a.max_row_nnz : 27) * sizeof(double);
-  const int cb = (int)nblocks(a.nC, 128), gb = (int)nblocks(a.ngen, 128);
-  const int sb = (int)nblocks(a.nS, 64), gcb = (int)nblocks(a.ngc, 64);
   if (events) CUDA_TRY(cudaEventRecord(events[0], st));
   {
     const int nchunks = (int)nblocks(a.nc + a.nb, 32);
     state_kernel<<<nblocks((long long)nchunks * 32, 256), 256, 0, st>>>(a, nchunks, chunk_multiplier(nchunks));
   }
   if (events) CUDA_TRY(cudaEventRecord(events[1], st));
-  if (cb + gb > 0) {
+  {
+    // mostly other vertices (e.g. prisms, whose valence-4 vertices are
+    // canonical): the warp form in its own launch, then the canonical ones;
+    // else one launch with the thread form in the first blocks
+    const bool gen_warp = a.ngen > a.nC;
+    if (gen_warp) {
+      const size_t gen_smem = (size_t)kGenWarps * a.gen_warp_doubles * sizeof(double);
+      generic_vertex_kernel<<<nblocks(a.ngen, kGenWarps), 128, gen_smem, st>>>(a);
+    }
+    const size_t canon_smem = 36 * 128 * sizeof(double);
+    const int cb = (int)nblocks(a.nC, 128), gb = gen_warp ? 0 : (int)nblocks(a.ngen, 128);
     const bool cr = a.rho_type != WATER_DENSITY_EXPONENTIAL;
-    if (cr && a.jac_ff)
-      vertex_kernel<true, true><<<cb + gb, 128, canon_smem, st>>>(a, gb);
-    else if (cr)
-      vertex_kernel<true, false><<<cb + gb, 128, canon_smem, st>>>(a, gb);
-    else if (a.jac_ff)
-      vertex_kernel<false, true><<<cb + gb, 128, canon_smem, st>>>(a, gb);
-    else
-      vertex_kernel<false, false><<<cb + gb, 128, canon_smem, st>>>(a, gb);
-  }
-  if (events) CUDA_TRY(cudaEventRecord(events[2], st));
-  if (cell_smem > 48 * 1024) {
-    // rows longer than 96 entries: opt in to more dynamic shared memory
-    static thread_local size_t granted = 48 * 1024;
-    if (cell_smem > granted) {
-      CUDA_TRY(cudaFuncSetAttribute(cell_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cell_smem));
-      granted = cell_smem;
+    if (cb + gb > 0) {
+      if (cr && a.jac_ff)
+        vertex_kernel<true, true><<<cb + gb, 128, canon_smem, st>>>(a, gb);
+      else if (cr)
+        vertex_kernel<true, false><<<cb + gb, 128, canon_smem, st>>>(a, gb);
+      else if (a.jac_ff)
+        vertex_kernel<false, true><<<cb + gb, 128, canon_smem, st>>>(a, gb);
+      else
+        vertex_kernel<false, false><<<cb + gb, 128, canon_smem, st>>>(a, gb);
     }
   }
-  if (sb + gcb > 0) cell_kernel<<<sb + gcb, 64, cell_smem, st>>>(a, sb);
+  if (events) CUDA_TRY(cudaEventRecord(events[2], st));
+  {
+    // the same choice for the cells: mostly other cells take the warp form
+    const bool gen_warp = a.ngc > a.nS;
+    const size_t cell_smem = 64 * (size_t)(gen_warp || a.max_row_nnz < 27 ? 27 : a.max_row_nnz) * sizeof(double);
+    const int sb = (int)nblocks(a.nS, 64), gcb = gen_warp ? 0 : (int)nblocks(a.ngc, 64);
+    if (cell_smem > 48 * 1024) {
+      // rows longer than 96 entries: opt in to more dynamic shared memory
+      static thread_local size_t granted = 48 * 1024;
+      if (cell_smem > granted) {
+        CUDA_TRY(cudaFuncSetAttribute(cell_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cell_smem));
+        granted = cell_smem;
+      }
+    }
+    if (sb + gcb > 0) cell_kernel<<<sb + gcb, 64, cell_smem, st>>>(a, sb);
+    if (gen_warp) {
+      const size_t gcell_smem = (size_t)kCellWarps * (size_t)a.max_row_nnz * sizeof(double);
+      generic_cell_kernel<<<nblocks(a.ngc, kCellWarps), 32 * kCellWarps, gcell_smem, st>>>(a);
+    }
+  }
   if (events) CUDA_TRY(cudaEventRecord(events[3], st));
   CUDA_TRY(cudaGetLastError());
   return 0;
@@ -1247,7 +1426,10 @@ int device_eval_noalloc(_p_TDy *t, const double *dU, double *dR, double *dJ, voi
 
 int device_launches_per_eval(_p_TDy *t) {
   const DevArgs &a = t->dev->a;
-  return 1 + ((a.nC + a.ngen) > 0 ? 1 : 0) + ((a.nS + a.ngc) > 0 ? 1 : 0);
+  const bool vw = a.ngen > a.nC, cw = a.ngc > a.nS;
+  const int nvert = vw ? (a.ngen > 0) + (a.nC > 0) : ((a.nC + a.ngen) > 0 ? 1 : 0);
+  const int ncell = cw ? (a.ngc > 0) + (a.nS > 0) : ((a.nS + a.ngc) > 0 ? 1 : 0);
+  return 1 + nvert + ncell;
 }
 
 int device_synchronize(_p_TDy *t) {
