@@ -144,15 +144,18 @@ __device__ __forceinline__ void saturation(int type, const double *par, double S
       *dS = 0;
       *d2S = 0.0;
     } else {
+      // PressureSaturation_VanGenuchten (tdycharacteristiccurves.c:692-717)
+      // with two powers instead of four: (1 + x^n)^(m+1) = (1 + x^n) / Se and
+      // (1 + x^n)^(-m-2) = Se / (1 + x^n)^2 (FP64 pow is the cost here)
       double n = 1 / (1 - m);
       double pc_alpha = Pc * alpha;
       double pc_alpha_n = pow(pc_alpha, n);
       double one_plus = 1 + pc_alpha_n;
       double Se = pow(one_plus, -m);
       *S = (1.0 - Sr) * Se + Sr;
-      double dSe_dPc = -m * n * alpha * pc_alpha_n / (pc_alpha * pow(one_plus, m + 1));
+      double dSe_dPc = -m * n * alpha * pc_alpha_n * Se / (pc_alpha * one_plus);
       *dS = -dSe_dPc * (1.0 - Sr);
-      double d2Se = m * n * (pc_alpha_n)*pow(one_plus, -m - 2.0) * ((m * n + 1.0) * pc_alpha_n - n + 1) / (Pc * Pc);
+      double d2Se = m * n * pc_alpha_n * (Se / (one_plus * one_plus)) * ((m * n + 1.0) * pc_alpha_n - n + 1) / (Pc * Pc);
       *d2S = (1.0 - Sr) * d2Se;
     }
   } else {
@@ -185,13 +188,16 @@ __device__ __forceinline__ void relperm(int type, const double *p, double Se, do
       *Kr = 1.0;
       *dKr = 0.0;
       if (Se >= 1.0) return;
+      // two powers instead of five: Se^(1/m - 1/2) = so / sqrt(Se),
+      // (1 - so)^(m-1) = tmp / (1 - so), (1 - so)^m = tmp
       double so = pow(Se, 1 / m);
-      double tmp = pow(1 - so, m);
-      double kr = sqrt(Se);
-      kr *= (1 - tmp) * (1 - tmp);
+      double oms = 1 - so;
+      double tmp = pow(oms, m);
+      double sq = sqrt(Se);
+      double kr = sq * ((1 - tmp) * (1 - tmp));
       *Kr = kr;
       double d = 0.5 * kr / Se;
-      d += 2 * pow(Se, 1 / m - 0.5) * pow(1 - so, m - 1) * (1 - pow(1 - so, m));
+      d += 2 * (so / sq) * (tmp / oms) * (1 - tmp);
       *dKr = d;
     }
   } else {
