@@ -471,6 +471,34 @@ def prisms_eval_full_size(ntri=200_000, nlayers=40, reps=10, dt=3600.0):
                     "N(0, 50 Pa) from it; errors in units of the oracle's per-entry error scale"}
 
 
+def profile_prisms(ntri, evaluations, dt=3600.0):
+    """Only the device F+J of the prism workload (3-D rotated K, a state with
+    saturated and unsaturated cells), ``evaluations`` times, for profilers."""
+    import torch
+
+    import tdycore_gb300 as T
+    from tdycore_gb300.workloads import infiltration_prisms
+
+    T.options_clear()
+    t, U0, top, src, info = infiltration_prisms(ntri, 40, rotation="full")
+    t.setup()
+    t.set_source_sink_values(src, cells=top)
+    nc, nnz = t.ncells, int(t.nnz)
+    dev = torch.device("cuda")
+    st = torch.cuda.Stream(device=dev)
+    U = U0 + 2.0e4 + np.random.default_rng(5).normal(0.0, 2.0e3, nc)
+    dU = torch.tensor(U, dtype=torch.float64, device=dev)
+    dUp = dU + 10.0
+    dR = torch.empty(nc, dtype=torch.float64, device=dev)
+    dJ = torch.empty(nnz, dtype=torch.float64, device=dev)
+    t.set_dtime(dt)
+    t.presolve_device(dUp, stream=st.cuda_stream)
+    for _ in range(evaluations):
+        t.snes_function_jacobian_device(dU, dR, dJ, stream=st.cuda_stream)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_run": info["workload"], "ncells": nc, "nnz": nnz, "evaluations": evaluations}))
+
+
 def serving_config5(nreq=160, rate=80.0, slots=32):
     """Config 5: Poisson arrivals of column/subdomain requests (5 % of them
     64 x 64 x 50 cells), 24 hourly backward-Euler steps each with top-flux
@@ -789,13 +817,18 @@ def main():
                          "(200000 is the full configuration; 0 skips it)")
     ap.add_argument("--batch-instances", type=int, default=4096,
                     help="instances of the batched-solve measurement (0 skips it)")
+    ap.add_argument("--profile-prisms", type=int, default=0, metavar="NTRI",
+                    help="only --steps device F+J evaluations of the prism workload with NTRI surface "
+                         "triangles and 40 layers (for ncu)")
     ap.add_argument("--profile", action="store_true",
                     help="time the device loop only (no timers, e2e, CPU or clock-fill loops), for ncu")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
-    if args.impl == "reference":
+    if args.profile_prisms > 0:
+        profile_prisms(args.profile_prisms, args.steps)
+    elif args.impl == "reference":
         run_reference(args, rank)
     else:
         run_gpu(args, rank, world, local_rank)

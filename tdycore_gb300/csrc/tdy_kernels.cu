@@ -1,7 +1,7 @@
 // tdy_kernels.cu -- sm_103a kernels of the MPFA-O Richards residual and
 // Jacobian, and their host-side launch code.
 //
-// One evaluation is three launches on one stream:
+// One evaluation is three stages on one stream:
 //   1. state_kernel   (cells, then boundary faces)
 //        TDyUpdateState_Richards_MPFAO (src/fv/mpfao/tdympfao.c:2527-2594),
 //        TDyMPFAO_SetBoundaryPressure + TDyMPFAOUpdateBoundaryState
@@ -9,23 +9,25 @@
 //        terms of TDyMPFAOSNESFunction/Jacobian (tdympfao_snes.c:19-30,
 //        112-123, 166-179) or TDyMPFAOIFunction/IJacobian_Accumulation
 //        (tdympfao_ts.c:191-212, 459-517).
-//   2. vertex_kernel  (one thread per vertex; interior hexahedral vertices
-//                      first, in their own blocks, then the others)
-//        MatMult(Trans_mat, P_vec) (tdympfao_ts.c:184) restricted to the
-//        vertex's rows, the upwinded flux of TDyMPFAOIFunction_Vertices
+//   2. vertices: MatMult(Trans_mat, P_vec) (tdympfao_ts.c:184) restricted to
+//        the vertex's rows, the upwinded flux of TDyMPFAOIFunction_Vertices
 //        (tdympfao_ts.c:12-150) and the Jacobian entries of
 //        TDyMPFAOIJacobian_Vertices (tdympfao_ts.c:235-456).  Each vertex
 //        writes its partial residual R_v[nint] and partial Jacobian block
 //        J_v[nint][nint] (rows and columns: the vertex's internal cells) to a
 //        scratch area it alone owns.  Interior hexahedral vertices use a fixed
 //        octant layout (rows and columns known at compile time, structure-of-
-//        arrays storage read with coalesced loads); the rest use per-vertex
-//        blocks.
-//   3. cell_kernel    (one thread per cell)
-//        sums, in a fixed order, the partials of the cell's vertices into
-//        R[cell] and into the cell's row of the fixed CSR pattern, then adds
-//        the accumulation terms.  No atomics: results are bitwise
-//        reproducible run to run.
+//        arrays storage read with coalesced loads, one thread each, in
+//        vertex_kernel); the others use per-vertex blocks, one thread each in
+//        the first blocks of vertex_kernel when canonical vertices dominate,
+//        else one warp each in generic_vertex_kernel (a launch of its own).
+//   3. cells: sum, in a fixed order, the partials of the cell's vertices into
+//        R[cell] and into the cell's row of the fixed CSR pattern, then add
+//        the accumulation terms (cell_kernel: structured cells, and the
+//        others one thread each when structured cells dominate; else the
+//        others one warp each in generic_cell_kernel).  No atomics, and the
+//        thread and warp forms sum in the same order: results are bitwise
+//        reproducible run to run and independent of the form.
 //
 // Per row the flux is evaluated as -w*(T.P + rho_avg*G) with w = rho_avg*kr/mu
 // and the Jacobian entry as -(w*T + E) with E the derivative terms of the
@@ -1102,6 +1104,7 @@ void device_destroy(_p_TDy *t) {
   if (d->stream) cudaStreamSynchronize(d->stream);
   for (int k = 0; k < 4; k++)
     if (d->ev[k]) cudaEventDestroy(d->ev[k]);
+
   for (void *p : d->allocs) cudaFree(p);
   if (d->stream) cudaStreamDestroy(d->stream);
   delete d;

@@ -241,3 +241,21 @@ def test_long_jacobian_rows_prisms():
     Jr, Jm = o.snes_jacobian(U, with_mag=True)
     assert_close(R, Rr, Rm, R_TOL, "prisms SNES residual")
     assert_close(J, Jr, Jm, J_TOL, "prisms SNES Jacobian")
+
+
+@pytest.mark.parametrize("name", ["spe10_small", "wedge"])
+def test_pinned_and_pageable_host_buffers(name):
+    """Caller-owned page-locked R and J (as the benchmark's end-to-end loop
+    passes) receive the same bits from the host-pointer call as pageable
+    arrays allocated by the binding."""
+    import torch
+
+    t, o, U, Uprev, Ut = _setup(name)
+    t.set_dtime(DT)
+    t.presolve(Uprev)
+    R1, J1 = t.snes_function_jacobian(U)
+    Rp = torch.full((t.ncells,), float("nan"), dtype=torch.float64).pin_memory()
+    Jp = torch.full((t.nnz,), float("nan"), dtype=torch.float64).pin_memory()
+    t.snes_function_jacobian(U, Rp.numpy(), Jp.numpy())
+    assert np.array_equal(Rp.numpy(), R1)
+    assert np.array_equal(Jp.numpy(), J1)
