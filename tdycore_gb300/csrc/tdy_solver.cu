@@ -446,7 +446,8 @@ int autotune_spmv(SolverState *s, Krylov &k, cudaStream_t st) {
 }
 
 template <class T>
-int linear_solve(SolverState *s, Krylov &k, const TDyNewtonOptions &o, cudaStream_t st, long long *lin_total) {
+int linear_solve(SolverState *s, Krylov &k, const TDyNewtonOptions &o, cudaStream_t st, long long *lin_total,
+                 std::vector<int> &inst_lin_its) {
   int ierr;
   if ((ierr = krylov_alloc<T>(s, k))) return ierr;
   if ((ierr = autotune_spmv<T>(s, k, st))) return ierr;  // uses b and v as scratch before they are set
@@ -487,6 +488,7 @@ int linear_solve(SolverState *s, Krylov &k, const TDyNewtonOptions &o, cudaStrea
   SCUDA(cudaMemcpyAsync(its.data(), s->lin_its, sizeof(int) * ns, cudaMemcpyDeviceToHost, st));
   SCUDA(cudaStreamSynchronize(st));
   for (int v : its) *lin_total += v;
+  inst_lin_its = its;
   return 0;
 }
 
@@ -589,6 +591,7 @@ int device_be_solve(_p_TDy *t, double dt, double *dU, const TDyNewtonOptions &o,
   std::vector<double> f0(ns, 0.0), fn(ns, 0.0), g2(ns, 0.0), lam(ns, 1.0);
   std::vector<int> act(ns, 1), its(ns, 0), trial(ns, 0), commit(ns, 0), step_conv(ns, 0), failed(ns, 0);
   std::vector<double> y2(ns, 0.0), x2(ns, 0.0);
+  std::vector<int> lin_its(ns, 0);  // inner iterations of the last solve, per instance
   long long lin_total = 0;
   // F and J at x (= xb for every instance after each evaluation below), and
   // the squared per-instance residual norms into g2
@@ -604,6 +607,7 @@ int device_be_solve(_p_TDy *t, double dt, double *dU, const TDyNewtonOptions &o,
   if ((ierr = evaluate())) return ierr;
   for (int g = 0; g < ns; g++) f0[g] = fn[g] = std::sqrt(g2[g]);
   const double alpha = 1e-4;  // sufficient-decrease constant of PETSc's backtracking line search
+  constexpr double kMaxStep = 1e8;  // PETSc's default SNESLineSearch maxstep
   const int max_backtracks = 12;
   for (int it = 0;; it++) {
     bool any = false;
@@ -624,19 +628,36 @@ int device_be_solve(_p_TDy *t, double dt, double *dU, const TDyNewtonOptions &o,
     SCUDA(cudaMemcpyAsync(s->newt_active, act.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, st));
     const void *y;
     if (o.linear_fp32) {
-      ierr = linear_solve<float>(s, s->k32, o, st, &lin_total);
+      ierr = linear_solve<float>(s, s->k32, o, st, &lin_total, lin_its);
       y = s->k32.y;
     } else {
-      ierr = linear_solve<double>(s, s->k64, o, st, &lin_total);
+      ierr = linear_solve<double>(s, s->k64, o, st, &lin_total, lin_its);
       y = s->k64.y;
     }
     if (ierr) return ierr;
+    // ||y|| and ||x|| before the step: PETSc's backtracking line search caps
+    // the step at maxstep and ends with convergence by the step test when the
+    // full step fails and ||y|| < stol ||x||
+    {
+      if (o.linear_fp32)
+        seg_dot<float, float>(s, (const float *)y, (const float *)y, nullptr, nullptr, s->fn2, nullptr, st);
+      else
+        seg_dot<double, double>(s, (const double *)y, (const double *)y, nullptr, nullptr, s->fn2, nullptr, st);
+      seg_dot<double, double>(s, s->xb, s->xb, nullptr, nullptr, s->scal + (size_t)S_T2 * ns, nullptr, st);
+      SCUDA(cudaGetLastError());
+      SCUDA(cudaMemcpyAsync(y2.data(), s->fn2, sizeof(double) * ns, cudaMemcpyDeviceToHost, st));
+      SCUDA(cudaMemcpyAsync(x2.data(), s->scal + (size_t)S_T2 * ns, sizeof(double) * ns, cudaMemcpyDeviceToHost, st));
+      SCUDA(cudaStreamSynchronize(st));
+    }
     // backtracking per instance: accept when ||F(x - lam y)||^2 <= (1 - 2 alpha lam) ||F(x)||^2
     // (initial slope -||F||^2 of the Newton direction), else a quadratic fit of
     // lam clamped to [0.1 lam, 0.5 lam] (PETSc SNESLineSearchApply_BT)
     for (int g = 0; g < ns; g++) {
       trial[g] = act[g];
-      lam[g] = 1.0;
+      // ||lam y|| <= maxstep (SNESLineSearch maxstep, PETSc default 1e8): a
+      // direction from a diverged inner solve cannot throw the state away
+      const double yn = std::sqrt(y2[g]);
+      lam[g] = yn > kMaxStep ? kMaxStep / yn : 1.0;
     }
     for (int ls = 0; ls <= max_backtracks; ls++) {
       SCUDA(cudaMemcpyAsync(s->trial, trial.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, st));
@@ -653,20 +674,28 @@ int device_be_solve(_p_TDy *t, double dt, double *dU, const TDyNewtonOptions &o,
         commit[g] = 0;
         if (!trial[g]) continue;
         const double f = fn[g] * fn[g], gg = g2[g];
-        if (std::isfinite(gg) && (gg <= (1.0 - 2.0 * alpha * lam[g]) * f || (ls == max_backtracks && gg <= 4.0 * f))) {
-          // sufficient decrease; or, at the smallest step, ||F|| at most
-          // doubled (at the FP64 noise floor no step lowers ||F||; the step
-          // test or the iteration limit then ends the instance)
+        const bool inner_ok = lin_its[g] < o.linear_max_it;
+        if (std::isfinite(gg) &&
+            (gg <= (1.0 - 2.0 * alpha * lam[g]) * f || (ls == max_backtracks && (inner_ok || gg <= 4.0 * f)))) {
+          // sufficient decrease; or, at the smallest step, a Newton direction
+          // from a converged inner solve (the next iteration's Jacobian at the
+          // nearby state usually gives a better one; at the FP64 noise floor
+          // no step lowers ||F|| and the step test ends the instance), or one
+          // from an unconverged inner solve that at most doubles ||F||
           commit[g] = 1;
           trial[g] = 0;
           fn[g] = std::sqrt(gg);
         } else if (ls == max_backtracks) {
-          // line search failure: even the smallest step more than doubles
-          // ||F|| (a direction from an inner solve that did not converge);
-          // keep the last accepted state, stop
+          // no finite residual along the step, or an unconverged inner solve
+          // whose smallest step more than doubles ||F||: keep the last
+          // accepted state and stop, converged by the step test if the step
+          // is negligible, else failed
           trial[g] = 0;
           act[g] = 0;
-          failed[g] = 1;
+          if (o.stol > 0.0 && std::sqrt(y2[g]) < o.stol * std::sqrt(x2[g]))
+            step_conv[g] = 1;
+          else
+            failed[g] = 1;
         } else {
           const double slope = -f;
           double lt = std::isfinite(gg) ? -slope * lam[g] * lam[g] / (gg - f - 2.0 * slope * lam[g]) : 0.0;
