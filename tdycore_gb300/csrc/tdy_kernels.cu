@@ -79,8 +79,8 @@ struct DevArgs {
   // faces
   const int *f_up, *f_dn;
   const double *G;
-  // canonical interior-hex vertices (SoA, stride nCpad)
-  int nC, nCpad;
+  // canonical interior-hex vertices (SoA, stride nCpad); a launch takes those in [vc0, vc1)
+  int nC, nCpad, vc0, vc1;
   const double *Tc;
   int jac_ff;  // Jacobian products of canonical vertices in double-float
   const int *cellc, *facec;
@@ -122,6 +122,19 @@ struct DeviceState {
   double *diagS = nullptr, *diagMass = nullptr;
   double *dae = nullptr;  // DAE form: U, U_t, R interleaved (6 * nc), on first use
   int nnz = 0;
+  // host-pointer evaluations in slabs of cells (see build_slabs): each slab's
+  // rows of R and J go to host memory while the next slabs are evaluated
+  struct Slab {
+    int c0, c1;        // cells
+    int vc0, vc1;      // canonical vertices
+    int g0, g1;        // other vertices (indices into gen_vertex)
+    int s0, s1;        // structured cells (indices into sc_cells)
+    int gc0, gc1;      // other cells (indices into gc_cells)
+    long long j0, j1;  // Jacobian values
+  };
+  std::vector<Slab> slabs;
+  cudaStream_t copy_stream = nullptr;
+  std::vector<cudaEvent_t> slab_ev;
 };
 
 #define CUDA_TRY(call)                                                                          \
@@ -447,8 +460,8 @@ template <bool CONST_RHO, bool FFJ>
 __device__ __forceinline__ void canon_vertex(const DevArgs &a, int block) {
   extern __shared__ double sh[];  // [36][blockDim]: w, E_up, E_dn per row
   const int tid = threadIdx.x, bs = blockDim.x;
-  const int vc = block * bs + tid;
-  if (vc >= a.nC) return;
+  const int vc = a.vc0 + block * bs + tid;
+  if (vc >= a.vc1) return;
   const long long P = a.nCpad;
   double p[8], hr[8], lam[8], dlam[8], hdr[8];
 #pragma unroll
@@ -967,6 +980,59 @@ static int dupload(DeviceState *d, T **p, const std::vector<T> &h) {
   return 0;
 }
 
+// Slabs of the host-pointer evaluation, for a single extruded block (cells
+// numbered layer by layer): cells split at layer boundaries into up to eight
+// slabs; a vertex belongs to the slab of the first cell that uses it, so the
+// cells of slab k need only vertices of slabs <= k.  The vertex and cell
+// lists (ascending indices) must then run through the slabs in order, which
+// is checked: any other numbering leaves one slab (no pipelining).
+static void build_slabs(_p_TDy *t, DeviceState *d) {
+  d->slabs.clear();
+  if (t->mesh_blocks.size() != 1) return;
+  const ExtrudedInput &blk = t->mesh_blocks[0];
+  const Mesh &m = t->mesh;
+  const MPFAOSetup &s = t->setup;
+  const int nl = blk.nlayers, nc2 = blk.nc2;
+  const int K = std::min(8, nl / 4);
+  if (K < 2 || m.nc != nl * nc2) return;
+  std::vector<int> cut(K + 1);
+  for (int k = 0; k <= K; k++) cut[k] = (int)((long long)k * nl / K) * nc2;
+  auto slab_of_cell = [&](int c) { return (int)(std::upper_bound(cut.begin(), cut.end(), c) - cut.begin()) - 1; };
+  auto slab_of_vertex = [&](int v) { return slab_of_cell(m.vert_cells[m.vert_cell_off[v]]); };
+  // b[k] = first list index in slab k or later; false if the slab decreases
+  auto bounds = [&](const std::vector<int> &list, auto slab_of, std::vector<int> &b) {
+    b.assign(K + 1, (int)list.size());
+    b[0] = 0;
+    int cur = 0;
+    for (int i = 0; i < (int)list.size(); i++) {
+      const int sk = slab_of(list[i]);
+      if (sk < cur) return false;
+      while (cur < sk) b[++cur] = i;
+    }
+    return true;
+  };
+  std::vector<int> bc, bg, bs, bgc;
+  if (!bounds(s.canon_vertex, slab_of_vertex, bc) || !bounds(s.gen_vertex, slab_of_vertex, bg) ||
+      !bounds(s.sc_cells, slab_of_cell, bs) || !bounds(s.gc_cells, slab_of_cell, bgc))
+    return;
+  for (int k = 0; k < K; k++) {
+    DeviceState::Slab sl;
+    sl.c0 = cut[k];
+    sl.c1 = cut[k + 1];
+    sl.vc0 = bc[k];
+    sl.vc1 = bc[k + 1];
+    sl.g0 = bg[k];
+    sl.g1 = bg[k + 1];
+    sl.s0 = bs[k];
+    sl.s1 = bs[k + 1];
+    sl.gc0 = bgc[k];
+    sl.gc1 = bgc[k + 1];
+    sl.j0 = s.rowptr[cut[k]];
+    sl.j1 = s.rowptr[cut[k + 1]];
+    d->slabs.push_back(sl);
+  }
+}
+
 int device_setup(_p_TDy *t) {
   const Mesh &m = t->mesh;
   const MPFAOSetup &s = t->setup;
@@ -1028,6 +1094,8 @@ int device_setup(_p_TDy *t) {
   UP(a.f_dn, fdn);
   UP(a.G, s.gravdis);
   a.nC = s.nC;
+  a.vc0 = 0;
+  a.vc1 = s.nC;
   a.nCpad = s.nCpad;
   if (t->opt.setup_on_device) {
     double *tc;
@@ -1094,6 +1162,12 @@ int device_setup(_p_TDy *t) {
   if ((ierr = dalloc(d, &d->dJ, d->nnz))) return ierr;
   if ((ierr = dalloc(d, &d->diagS, m.nc))) return ierr;
   if ((ierr = dalloc(d, &d->diagMass, m.nc))) return ierr;
+  build_slabs(t, d);
+  if (d->slabs.size() > 1) {
+    CUDA_TRY(cudaStreamCreateWithFlags(&d->copy_stream, cudaStreamNonBlocking));
+    d->slab_ev.assign(d->slabs.size(), nullptr);
+    for (cudaEvent_t &e : d->slab_ev) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  }
   CUDA_TRY(cudaDeviceSynchronize());
   return 0;
 }
@@ -1104,6 +1178,11 @@ void device_destroy(_p_TDy *t) {
   if (d->stream) cudaStreamSynchronize(d->stream);
   for (int k = 0; k < 4; k++)
     if (d->ev[k]) cudaEventDestroy(d->ev[k]);
+  if (d->copy_stream) {
+    cudaStreamSynchronize(d->copy_stream);
+    cudaStreamDestroy(d->copy_stream);
+  }
+  for (cudaEvent_t e : d->slab_ev) cudaEventDestroy(e);
 
   for (void *p : d->allocs) cudaFree(p);
   if (d->stream) cudaStreamDestroy(d->stream);
@@ -1157,66 +1236,81 @@ int device_presolve_host(_p_TDy *t, const double *Uprev) {
 
 // The four launches of one evaluation; events[] (5 entries, or null) bracket
 // them for the per-kernel timers.
+static int launch_state(const DevArgs &a, cudaStream_t st) {
+  const int nchunks = (int)nblocks(a.nc + a.nb, 32);
+  state_kernel<<<nblocks((long long)nchunks * 32, 256), 256, 0, st>>>(a, nchunks, chunk_multiplier(nchunks));
+  return 0;
+}
+
+// Vertex stage over the vertices a names (gen_vertex/ngen, [vc0, vc1)).
+// gen_warp: mostly other vertices (e.g. prisms, whose valence-4 vertices are
+// canonical): the warp form in its own launch, then the canonical ones; else
+// one launch with the thread form in the first blocks.  The choice is made
+// once per mesh, so a slab launches the same form as the whole evaluation.
+static int launch_vertices(const DevArgs &a, bool gen_warp, cudaStream_t st) {
+  if (gen_warp && a.ngen > 0) {
+    const size_t gen_smem = (size_t)kGenWarps * a.gen_warp_doubles * sizeof(double);
+    generic_vertex_kernel<<<nblocks(a.ngen, kGenWarps), 128, gen_smem, st>>>(a);
+  }
+  const size_t canon_smem = 36 * 128 * sizeof(double);
+  const int cb = (int)nblocks(a.vc1 - a.vc0, 128), gb = gen_warp ? 0 : (int)nblocks(a.ngen, 128);
+  const bool cr = a.rho_type != WATER_DENSITY_EXPONENTIAL;
+  if (cb + gb > 0) {
+    if (cr && a.jac_ff)
+      vertex_kernel<true, true><<<cb + gb, 128, canon_smem, st>>>(a, gb);
+    else if (cr)
+      vertex_kernel<true, false><<<cb + gb, 128, canon_smem, st>>>(a, gb);
+    else if (a.jac_ff)
+      vertex_kernel<false, true><<<cb + gb, 128, canon_smem, st>>>(a, gb);
+    else
+      vertex_kernel<false, false><<<cb + gb, 128, canon_smem, st>>>(a, gb);
+  }
+  return 0;
+}
+
+// Cell stage over the cells a names (sc_cells/nS, gc_cells/ngc); gen_warp:
+// mostly other cells take the warp form.
+static int launch_cells(const DevArgs &a, bool gen_warp, cudaStream_t st) {
+  const size_t cell_smem = 64 * (size_t)(gen_warp || a.max_row_nnz < 27 ? 27 : a.max_row_nnz) * sizeof(double);
+  const int sb = (int)nblocks(a.nS, 64), gcb = gen_warp ? 0 : (int)nblocks(a.ngc, 64);
+  if (cell_smem > 48 * 1024) {
+    // rows longer than 96 entries: opt in to more dynamic shared memory
+    static thread_local size_t granted = 48 * 1024;
+    if (cell_smem > granted) {
+      CUDA_TRY(cudaFuncSetAttribute(cell_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cell_smem));
+      granted = cell_smem;
+    }
+  }
+  if (sb + gcb > 0) cell_kernel<<<sb + gcb, 64, cell_smem, st>>>(a, sb);
+  if (gen_warp && a.ngc > 0) {
+    const size_t gcell_smem = (size_t)kCellWarps * (size_t)a.max_row_nnz * sizeof(double);
+    generic_cell_kernel<<<nblocks(a.ngc, kCellWarps), 32 * kCellWarps, gcell_smem, st>>>(a);
+  }
+  return 0;
+}
+
+static bool vertex_warp_form(const DevArgs &a) { return a.ngen > a.nC; }
+static bool cell_warp_form(const DevArgs &a) { return a.ngc > a.nS; }
+
+// The stages of one evaluation; events[] (4 entries, or null) bracket them
+// for the per-kernel timers.
 static int launch_eval(const DevArgs &a, cudaStream_t st, cudaEvent_t *events) {
+  int ierr;
   if (events) CUDA_TRY(cudaEventRecord(events[0], st));
-  {
-    const int nchunks = (int)nblocks(a.nc + a.nb, 32);
-    state_kernel<<<nblocks((long long)nchunks * 32, 256), 256, 0, st>>>(a, nchunks, chunk_multiplier(nchunks));
-  }
+  if ((ierr = launch_state(a, st))) return ierr;
   if (events) CUDA_TRY(cudaEventRecord(events[1], st));
-  {
-    // mostly other vertices (e.g. prisms, whose valence-4 vertices are
-    // canonical): the warp form in its own launch, then the canonical ones;
-    // else one launch with the thread form in the first blocks
-    const bool gen_warp = a.ngen > a.nC;
-    if (gen_warp) {
-      const size_t gen_smem = (size_t)kGenWarps * a.gen_warp_doubles * sizeof(double);
-      generic_vertex_kernel<<<nblocks(a.ngen, kGenWarps), 128, gen_smem, st>>>(a);
-    }
-    const size_t canon_smem = 36 * 128 * sizeof(double);
-    const int cb = (int)nblocks(a.nC, 128), gb = gen_warp ? 0 : (int)nblocks(a.ngen, 128);
-    const bool cr = a.rho_type != WATER_DENSITY_EXPONENTIAL;
-    if (cb + gb > 0) {
-      if (cr && a.jac_ff)
-        vertex_kernel<true, true><<<cb + gb, 128, canon_smem, st>>>(a, gb);
-      else if (cr)
-        vertex_kernel<true, false><<<cb + gb, 128, canon_smem, st>>>(a, gb);
-      else if (a.jac_ff)
-        vertex_kernel<false, true><<<cb + gb, 128, canon_smem, st>>>(a, gb);
-      else
-        vertex_kernel<false, false><<<cb + gb, 128, canon_smem, st>>>(a, gb);
-    }
-  }
+  if ((ierr = launch_vertices(a, vertex_warp_form(a), st))) return ierr;
   if (events) CUDA_TRY(cudaEventRecord(events[2], st));
-  {
-    // the same choice for the cells: mostly other cells take the warp form
-    const bool gen_warp = a.ngc > a.nS;
-    const size_t cell_smem = 64 * (size_t)(gen_warp || a.max_row_nnz < 27 ? 27 : a.max_row_nnz) * sizeof(double);
-    const int sb = (int)nblocks(a.nS, 64), gcb = gen_warp ? 0 : (int)nblocks(a.ngc, 64);
-    if (cell_smem > 48 * 1024) {
-      // rows longer than 96 entries: opt in to more dynamic shared memory
-      static thread_local size_t granted = 48 * 1024;
-      if (cell_smem > granted) {
-        CUDA_TRY(cudaFuncSetAttribute(cell_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cell_smem));
-        granted = cell_smem;
-      }
-    }
-    if (sb + gcb > 0) cell_kernel<<<sb + gcb, 64, cell_smem, st>>>(a, sb);
-    if (gen_warp) {
-      const size_t gcell_smem = (size_t)kCellWarps * (size_t)a.max_row_nnz * sizeof(double);
-      generic_cell_kernel<<<nblocks(a.ngc, kCellWarps), 32 * kCellWarps, gcell_smem, st>>>(a);
-    }
-  }
+  if ((ierr = launch_cells(a, cell_warp_form(a), st))) return ierr;
   if (events) CUDA_TRY(cudaEventRecord(events[3], st));
   CUDA_TRY(cudaGetLastError());
   return 0;
 }
 
-int device_eval(_p_TDy *t, int form, double time, const double *dU, const double *dUt, double shift, double *dR,
-                double *dJ, void *stream) {
-  (void)time;
+// The arguments of one evaluation.
+static int eval_args(_p_TDy *t, int form, const double *dU, const double *dUt, double shift, double *dR, double *dJ,
+                     DevArgs *out) {
   DeviceState *d = t->dev;
-  cudaStream_t st = stream ? (cudaStream_t)stream : d->stream;
   if (form == FORM_SNES && !(t->dtime > 0.0))
     return set_error(TDY_ERR_USER, "SNES form needs TDySetDtimeForSNESSolver before evaluation");
   DevArgs a = d->a;
@@ -1229,7 +1323,19 @@ int device_eval(_p_TDy *t, int form, double time, const double *dU, const double
   a.needJ = dJ != nullptr;
   a.R = dR;
   a.J = dJ;
-  int ierr = launch_eval(a, st, d->timers ? d->ev : nullptr);
+  *out = a;
+  return 0;
+}
+
+int device_eval(_p_TDy *t, int form, double time, const double *dU, const double *dUt, double shift, double *dR,
+                double *dJ, void *stream) {
+  (void)time;
+  DeviceState *d = t->dev;
+  cudaStream_t st = stream ? (cudaStream_t)stream : d->stream;
+  DevArgs a;
+  int ierr = eval_args(t, form, dU, dUt, shift, dR, dJ, &a);
+  if (ierr) return ierr;
+  ierr = launch_eval(a, st, d->timers ? d->ev : nullptr);
   if (ierr) return ierr;
   if (d->timers) {
     CUDA_TRY(cudaEventSynchronize(d->ev[3]));
@@ -1362,6 +1468,42 @@ int device_eval_host(_p_TDy *t, int form, double time, const double *U, const do
   const size_t n = (size_t)t->mesh.nc;
   CUDA_TRY(cudaMemcpyAsync(d->dU, U, sizeof(double) * n, cudaMemcpyHostToDevice, d->stream));
   if (Ut) CUDA_TRY(cudaMemcpyAsync(d->dUt, Ut, sizeof(double) * n, cudaMemcpyHostToDevice, d->stream));
+  if (d->slabs.size() > 1 && J && !d->timers) {
+    // slab by slab: the vertex and cell stages of slab k, then its rows of R
+    // and J to host memory on the copy stream while slab k+1 is evaluated
+    // (the same launches, split; the same bits)
+    DevArgs a;
+    int ierr = eval_args(t, form, d->dU, Ut ? d->dUt : nullptr, shift, R ? d->dR : nullptr, d->dJ, &a);
+    if (ierr) return ierr;
+    const bool vw = vertex_warp_form(a), cw = cell_warp_form(a);
+    if ((ierr = launch_state(a, d->stream))) return ierr;
+    for (size_t k = 0; k < d->slabs.size(); k++) {
+      const DeviceState::Slab &sl = d->slabs[k];
+      DevArgs b = a;
+      b.gen_vertex = a.gen_vertex + sl.g0;
+      b.ngen = sl.g1 - sl.g0;
+      b.vc0 = sl.vc0;
+      b.vc1 = sl.vc1;
+      b.sc_cells = a.sc_cells + sl.s0;
+      b.sc_vc = a.sc_vc + sl.s0;  // structure of arrays, stride nSpad: the offset carries over
+      b.nS = sl.s1 - sl.s0;
+      b.gc_cells = a.gc_cells + sl.gc0;
+      b.ngc = sl.gc1 - sl.gc0;
+      if ((ierr = launch_vertices(b, vw, d->stream))) return ierr;
+      if ((ierr = launch_cells(b, cw, d->stream))) return ierr;
+      CUDA_TRY(cudaEventRecord(d->slab_ev[k], d->stream));
+      CUDA_TRY(cudaStreamWaitEvent(d->copy_stream, d->slab_ev[k], 0));
+      CUDA_TRY(cudaMemcpyAsync(J + sl.j0, d->dJ + sl.j0, sizeof(double) * (size_t)(sl.j1 - sl.j0),
+                               cudaMemcpyDeviceToHost, d->copy_stream));
+      if (R)
+        CUDA_TRY(cudaMemcpyAsync(R + sl.c0, d->dR + sl.c0, sizeof(double) * (size_t)(sl.c1 - sl.c0),
+                                 cudaMemcpyDeviceToHost, d->copy_stream));
+    }
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaStreamSynchronize(d->copy_stream));
+    CUDA_TRY(cudaStreamSynchronize(d->stream));
+    return 0;
+  }
   int ierr = device_eval(t, form, time, d->dU, Ut ? d->dUt : nullptr, shift, R ? d->dR : nullptr, J ? d->dJ : nullptr,
                          d->stream);
   if (ierr) return ierr;
