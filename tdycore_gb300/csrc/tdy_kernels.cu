@@ -981,7 +981,7 @@ static int dupload(DeviceState *d, T **p, const std::vector<T> &h) {
 }
 
 // Slabs of the host-pointer evaluation, for a single extruded block (cells
-// numbered layer by layer): cells split at layer boundaries into up to eight
+// numbered layer by layer): cells split at layer boundaries into up to four
 // slabs; a vertex belongs to the slab of the first cell that uses it, so the
 // cells of slab k need only vertices of slabs <= k.  The vertex and cell
 // lists (ascending indices) must then run through the slabs in order, which
@@ -993,7 +993,7 @@ static void build_slabs(_p_TDy *t, DeviceState *d) {
   const Mesh &m = t->mesh;
   const MPFAOSetup &s = t->setup;
   const int nl = blk.nlayers, nc2 = blk.nc2;
-  const int K = std::min(8, nl / 4);
+  const int K = std::min(4, nl / 4);
   if (K < 2 || m.nc != nl * nc2) return;
   std::vector<int> cut(K + 1);
   for (int k = 0; k <= K; k++) cut[k] = (int)((long long)k * nl / K) * nc2;
