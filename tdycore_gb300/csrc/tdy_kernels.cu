@@ -910,20 +910,26 @@ __device__ __forceinline__ void generic_cell_thread(const DevArgs &a, int block)
   }
 }
 
-// Other cells, warp form (meshes without structured cells): one warp per
-// cell.  The row is staged in shared memory; the lanes take the columns of
-// each vertex block (distinct columns land in distinct slots) and the
-// vertices are added in the cell's corner order, as in the thread form.
-constexpr int kCellWarps = 4;  // warps (cells) per generic-cell block
+// Other cells, warp form (meshes without structured cells): one half-warp
+// per cell (vertex blocks of such meshes have about 12 columns, so 16 lanes
+// keep the FP64 adds, this kernel's bound, mostly full).  The row is staged
+// in shared memory; the lanes take the columns of each vertex block (distinct
+// columns land in distinct slots) and the vertices are added in the cell's
+// corner order, as in the thread form.
+constexpr int kCellWarps = 4;  // warps per generic-cell block (two cells each)
 
 __device__ __forceinline__ void generic_cell_warp(const DevArgs &a, int block) {
-  extern __shared__ double rowbuf[];  // [kCellWarps][max_row_nnz]
+  extern __shared__ double rowbuf[];  // [2 * kCellWarps][max_row_nnz]
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int gidx = block * kCellWarps + warp;
-  if (gidx >= a.ngc) return;  // whole warp
+  const int half = lane >> 4, hl = lane & 15;
+  const int pair = block * kCellWarps + warp;
+  if (2 * pair >= a.ngc) return;  // whole warp
+  const int gidx = 2 * pair + half;
+  if (gidx >= a.ngc) return;  // the second half of the last warp
+  const unsigned mask = 0xffffu << (16 * half);
   const int i = a.gc_cells[gidx];
   const int k0 = a.cv_off[i], k1 = a.cv_off[i + 1];
-  if (a.needR && lane == 0) {
+  if (a.needR && hl == 0) {
     double s = 0.0;
     for (int k = k0; k < k1; k++) s += a.scratch[a.cv_rbase[k]];
     s += a.acc_a[i];
@@ -931,23 +937,23 @@ __device__ __forceinline__ void generic_cell_warp(const DevArgs &a, int block) {
     a.R[i] = s;
   }
   if (!a.needJ) return;
-  double *row = rowbuf + (size_t)warp * a.max_row_nnz;
+  double *row = rowbuf + (size_t)(2 * warp + half) * a.max_row_nnz;
   const int p0 = a.rowptr[i], rn = a.rowptr[i + 1] - p0;
-  for (int j = lane; j < rn; j += 32) row[j] = 0.0;
-  __syncwarp();
+  for (int j = hl; j < rn; j += 16) row[j] = 0.0;
+  __syncwarp(mask);
   int diag = -1;
   for (int k = k0; k < k1; k++) {
     const int nint = a.cv_nint[k], stride = a.cv_stride[k];
     const double *blk = a.scratch + a.cv_jbase[k];
     const unsigned char *sl = a.cv_slots + a.cv_slot_off[k];
-    for (int b = lane; b < nint; b += 32) row[sl[b]] += blk[(long long)b * stride];
+    for (int b = hl; b < nint; b += 16) row[sl[b]] += blk[(long long)b * stride];
     diag = sl[a.cv_local[k]];
-    __syncwarp();
+    __syncwarp(mask);
   }
-  if (lane == 0 && diag >= 0) row[diag] += a.jdiag[i];
-  __syncwarp();
+  if (hl == 0 && diag >= 0) row[diag] += a.jdiag[i];
+  __syncwarp(mask);
   double *out = a.J + p0;
-  for (int j = lane; j < rn; j += 32) out[j] = row[j];
+  for (int j = hl; j < rn; j += 16) out[j] = row[j];
 }
 
 __global__ void __launch_bounds__(64) cell_kernel(DevArgs a, int struct_blocks) {
@@ -1283,8 +1289,8 @@ static int launch_cells(const DevArgs &a, bool gen_warp, cudaStream_t st) {
   }
   if (sb + gcb > 0) cell_kernel<<<sb + gcb, 64, cell_smem, st>>>(a, sb);
   if (gen_warp && a.ngc > 0) {
-    const size_t gcell_smem = (size_t)kCellWarps * (size_t)a.max_row_nnz * sizeof(double);
-    generic_cell_kernel<<<nblocks(a.ngc, kCellWarps), 32 * kCellWarps, gcell_smem, st>>>(a);
+    const size_t gcell_smem = (size_t)2 * kCellWarps * (size_t)a.max_row_nnz * sizeof(double);
+    generic_cell_kernel<<<nblocks(a.ngc, 2 * kCellWarps), 32 * kCellWarps, gcell_smem, st>>>(a);
   }
   return 0;
 }
