@@ -125,12 +125,17 @@ def run_request(req: Request, fp32: bool = True, dt: float = 3600.0, rtol: float
         dU = torch.tensor(U0, dtype=torch.float64, device="cuda")
         torch.cuda.current_stream().synchronize()
         area = req.cell * req.cell
-        for q in req.forcing:
+        for k, q in enumerate(req.forcing):
             t.set_source_sink_values(np.full(top.size, RHO * q * area), cells=top)
             stats, its, rel = t.backward_euler_step_device(dU, dt, rtol=rtol, fp32=fp32)
             req.newton_its.append(int(its[0]))
             req.rel_residual.append(float(rel[0]))
-            req.converged_steps += int(stats["converged"])
+            if stats["converged"] != 1:
+                # the request ends here: later steps from an unconverged state
+                # would mean nothing to the caller
+                req.error = f"step {k + 1} did not converge (relative residual {rel[0]:.1e})"
+                break
+            req.converged_steps += 1
         req.U_final = dU.cpu().numpy()
     finally:
         t.destroy()
@@ -215,13 +220,16 @@ def make_requests(n: int, rate_per_s: float, nsteps: int = 24, large_fraction: f
 
 
 def summary(reqs, wall_s: float):
+    """Latency percentiles over the requests that completed; solves/s counts
+    converged solves only (a request ends at its first unconverged step)."""
     lat = np.array([r.latency_s for r in reqs if r.error is None])
     steps = sum(r.converged_steps for r in reqs)
-    total = sum(len(r.forcing) for r in reqs)
+    attempted = sum(len(r.rel_residual) for r in reqs)
     errs = [f"{r.rid}: {r.error}" for r in reqs if r.error is not None]
     return {"requests": len(reqs), "errors": len(errs), "error_messages": errs[:3],
             "p50_latency_s": float(np.percentile(lat, 50)) if lat.size else None,
             "p99_latency_s": float(np.percentile(lat, 99)) if lat.size else None,
-            "solves_per_s": total / wall_s, "converged_solves": steps, "solves": total,
+            "solves_per_s": steps / wall_s, "converged_solves": steps, "solves_attempted": attempted,
+            "solves_requested": sum(len(r.forcing) for r in reqs),
             "max_rel_residual": float(max((max(r.rel_residual) for r in reqs if r.rel_residual), default=0.0)),
             "wall_s": wall_s}

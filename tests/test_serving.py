@@ -1,6 +1,7 @@
 """Continuous-batching server: admission by slots and HBM budget in arrival
-order (CPU, with a stand-in runner), and on the GPU each request's result the
-same alone and in a mix, every step converged."""
+order (CPU, with a stand-in runner), the summary's counting rules (CPU), and
+on the GPU each request's result the same alone and in a mix, every step
+converged."""
 import threading
 import time
 
@@ -56,6 +57,25 @@ def test_request_generator_statistics():
     assert all(1 <= r.nx <= 8 and 1 <= r.ny <= 8 and 10 <= r.nz <= 100 for r in small)
     f = np.concatenate([r.forcing for r in reqs])
     assert abs(f.std() - 1e-7) < 1e-8
+
+
+def test_summary_counts_converged_solves_and_completed_requests():
+    """A request ends at its first unconverged step (reported as its error);
+    latency percentiles cover completed requests, solves/s converged solves."""
+    reqs = _requests(3, [4, 4, 4], [0.0, 0.0, 0.0])
+    for r in reqs:
+        r.forcing = np.zeros(3)
+        r.admitted_s, r.finished_s = r.arrival_s, r.arrival_s + 2.0
+    reqs[0].rel_residual, reqs[0].converged_steps = [1e-9, 1e-9, 1e-9], 3
+    reqs[1].rel_residual, reqs[1].converged_steps = [1e-9, 1e-9, 1e-9], 3
+    reqs[2].rel_residual, reqs[2].converged_steps = [1e-9, 0.5], 1
+    reqs[2].error = "step 2 did not converge (relative residual 5.0e-01)"
+    reqs[2].finished_s = reqs[2].arrival_s + 9.0
+    out = S.summary(reqs, wall_s=7.0)
+    assert out["errors"] == 1 and out["converged_solves"] == 7
+    assert out["solves_attempted"] == 8 and out["solves_requested"] == 9
+    assert out["solves_per_s"] == 1.0
+    assert out["p99_latency_s"] <= 2.0 + 1e-12
 
 
 @pytest.mark.gpu
