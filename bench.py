@@ -230,7 +230,7 @@ def batched_config4(ninst=4096, sample=64, dt=3600.0):
     3600 s to a relative FP64 residual of 1e-8 by the device Newton with
     FP32 Jacobian and inner solve, against the same instances solved one by
     one on the plain FP64 path (FP64 Jacobian and inner solve), timed on a
-    sample of them.  Every instance's result is judged by the FP64 oracle."""
+    sample of them.  Every instance's result is checked against the FP64 oracle."""
     import torch
 
     import tdycore_gb300 as T
@@ -394,7 +394,7 @@ def prisms_config3(ntri=20000, nlayers=40, steps=20, dt=20.0, rotation="vertical
     U = d.cpu().numpy()
     t.destroy()
     T.options_clear()
-    judged = [r for r in per_step if "oracle_rel_residual" in r]
+    checked = [r for r in per_step if "oracle_rel_residual" in r]
     return {
         "workload": info["workload"], "ncells": nc, "nnz_jacobian": nnz,
         "rotation": info["rotation"], "van_genuchten": info["van_genuchten"],
@@ -402,7 +402,7 @@ def prisms_config3(ntri=20000, nlayers=40, steps=20, dt=20.0, rotation="vertical
         "top_flux_m_per_s": info["top_flux_m_per_s"], "dt_s": dt, "steps": steps, "setup_s": setup_s,
         "mixed_s_total": mixed_s, "fp64_s_total": fp64_s, "speedup_mixed_vs_fp64": fp64_s / mixed_s,
         "all_converged_mixed": all(r["converged_mixed"] == 1 for r in per_step),
-        "max_oracle_rel_residual": max(r["oracle_rel_residual"] for r in judged),
+        "max_oracle_rel_residual": max(r["oracle_rel_residual"] for r in checked),
         "max_rel_diff_mixed_vs_fp64": max(r["max_rel_diff_mixed_vs_fp64"] for r in per_step),
         "pressure_range_pa_final": [float(U.min()), float(U.max())],
         "per_step": per_step,

@@ -1,6 +1,6 @@
 """Device-resident backward-Euler Newton solve (TDyBackwardEulerStepDevice).
 
-The judge of every result is the FP64 oracle: the oracle's SNES residual at
+Every result is checked against the FP64 oracle: the oracle's SNES residual at
 the returned state, relative to its residual at the start of the step, must
 meet the requested tolerance, whether the Jacobian and inner solve ran in FP32
 or FP64.  Batched instances must give each instance the same bits as solving
