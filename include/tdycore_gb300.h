@@ -212,8 +212,9 @@ TDyErrorCode TDyMPFAOIFunctionIJacobian(TDy tdy, double t, const double *U, cons
  * with the FP64 residual until ||F|| <= rtol ||F_0|| (or <= atol) per
  * instance (or until the Newton step is below stol ||U||, PETSc's step test),
  * with a backtracking line search per instance; each Newton system solved by BiCGStab preconditioned with exact
- * solves of the vertical lines of the extruded blocks, in FP32 (the Jacobian
- * is rounded to FP32) or FP64.  dU (device, ncells) holds U_n on entry and
+ * solves of the vertical lines of the extruded blocks or of strong-coupling
+ * clusters (TDyNewtonOptions.precond), in FP32 (the Jacobian is rounded to
+ * FP32) or FP64.  dU (device, ncells) holds U_n on entry and
  * U_{n+1} on return. */
 typedef struct {
   double rtol;         /* relative FP64 residual per instance (default 1e-8) */
@@ -224,7 +225,17 @@ typedef struct {
   int linear_max_it;   /* BiCGStab iterations per Newton iteration (default 400) */
   double stol;         /* step tolerance: converged when ||step|| < stol ||U|| per instance
                           (PETSc's CONVERGED_SNORM_RELATIVE; default 1e-8) */
+  int precond;         /* TDY_PRECOND_LINES (default) or TDY_PRECOND_CLUSTERS */
+  double cluster_threshold; /* clusters: a coupling with |a_ij| >= threshold sqrt(|a_ii a_jj|)
+                               joins cells i and j (default 0.05) */
 } TDyNewtonOptions;
+/* Inner-solve preconditioners.  LINES: exact solves of the vertical lines of
+ * the extruded blocks.  CLUSTERS: exact solves of the connected clusters of
+ * strong couplings (up to 64 cells each; cells of larger clusters take their
+ * diagonal), for meshes whose lateral couplings are not monotone (MPFA-O
+ * with anisotropic K on obtuse prisms), where line solves diverge. */
+#define TDY_PRECOND_LINES 0
+#define TDY_PRECOND_CLUSTERS 1
 typedef struct {
   int newton_iterations;        /* largest over the instances */
   long long linear_iterations;  /* BiCGStab iterations, summed over instances and Newton iterations */

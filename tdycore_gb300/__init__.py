@@ -67,7 +67,11 @@ class TDyMPFAOSetupView(ctypes.Structure):
 
 class NewtonOptions(ctypes.Structure):
     _fields_ = [("rtol", c_double), ("atol", c_double), ("max_it", c_int), ("linear_fp32", c_int),
-                ("linear_rtol", c_double), ("linear_max_it", c_int), ("stol", c_double)]
+                ("linear_rtol", c_double), ("linear_max_it", c_int), ("stol", c_double), ("precond", c_int),
+                ("cluster_threshold", c_double)]
+
+
+PRECOND_LINES, PRECOND_CLUSTERS = 0, 1
 
 
 class NewtonStats(ctypes.Structure):
@@ -607,15 +611,19 @@ class TDy:
         return n.value
 
     def backward_euler_step_device(self, dU, dt, rtol=1e-8, atol=0.0, max_it=50, fp32=True, linear_rtol=1e-6,
-                                   linear_max_it=400, stol=1e-8, stream=None):
+                                   linear_max_it=400, stol=1e-8, stream=None, precond="lines",
+                                   cluster_threshold=0.05):
         """One backward-Euler step of every instance with the device Newton
         solver; dU (device float64 tensor, ncells) holds U_n and receives
-        U_{n+1}.  Returns (stats dict, per-instance Newton iterations,
-        per-instance final ||F||/||F_0||)."""
+        U_{n+1}.  precond: "lines" or "clusters" (TDY_PRECOND_*).  Returns
+        (stats dict, per-instance Newton iterations, per-instance final
+        ||F||/||F_0||)."""
         o = NewtonOptions()
         check(lib.TDyNewtonOptionsDefault(byref(o)), "TDyNewtonOptionsDefault")
         o.rtol, o.atol, o.max_it, o.linear_fp32 = rtol, atol, max_it, int(bool(fp32))
         o.linear_rtol, o.linear_max_it, o.stol = linear_rtol, linear_max_it, stol
+        o.precond = {"lines": PRECOND_LINES, "clusters": PRECOND_CLUSTERS}[precond]
+        o.cluster_threshold = cluster_threshold
         st = NewtonStats()
         ni = self.num_instances()
         its = np.zeros(ni, dtype=np.int32)

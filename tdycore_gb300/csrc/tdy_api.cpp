@@ -1034,6 +1034,8 @@ TDyErrorCode TDyNewtonOptionsDefault(TDyNewtonOptions *o) {
   o->linear_rtol = 1e-6;
   o->linear_max_it = 400;
   o->stol = 1e-8;
+  o->precond = TDY_PRECOND_LINES;
+  o->cluster_threshold = 0.05;
   return 0;
 }
 TDyErrorCode TDyGetNumInstances(TDy tdy, int *n) {
@@ -1052,7 +1054,9 @@ TDyErrorCode TDyBackwardEulerStepDevice(TDy tdy, double dt, double *dU, const TD
   TDyNewtonOptions o;
   TDyNewtonOptionsDefault(&o);
   if (opt) o = *opt;
-  if (o.max_it < 0 || o.linear_max_it < 1 || !(o.rtol >= 0.0) || !(o.linear_rtol > 0.0))
+  if (o.max_it < 0 || o.linear_max_it < 1 || !(o.rtol >= 0.0) || !(o.linear_rtol > 0.0) ||
+      (o.precond != TDY_PRECOND_LINES && o.precond != TDY_PRECOND_CLUSTERS) ||
+      (o.precond == TDY_PRECOND_CLUSTERS && !(o.cluster_threshold > 0.0)))
     return set_error(TDY_ERR_ARG_OUTOFRANGE, "TDyBackwardEulerStepDevice: invalid options");
   return device_be_solve(tdy, dt, dU, o, stats, inst_iterations, inst_rel_residual, stream);
 }

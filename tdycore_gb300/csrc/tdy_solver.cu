@@ -49,8 +49,12 @@ struct Krylov {
   void *b = nullptr, *r = nullptr, *r0 = nullptr, *p = nullptr, *v = nullptr, *s = nullptr, *t = nullptr,
        *ph = nullptr, *sh = nullptr, *y = nullptr;     // vectors (T)
   void *la = nullptr, *lcp = nullptr, *linv = nullptr; // line factors (T)
+  void *cinv = nullptr;                                // clusters: 1/diagonal of the other cells (T)
+  void *clu = nullptr;                                 // clusters: LU factors (T), grown on demand
+  size_t clu_cap = 0;                                  // elements of clu
   cudaGraphExec_t graph = nullptr;
   cudaStream_t graph_stream = nullptr;
+  int graph_precond = -1;  // preconditioner the graph was captured with
   int tpr = 0;  // spmv threads per row (autotuned)
 };
 
@@ -68,11 +72,24 @@ struct SolverState {
   int *chunk_off = nullptr, *seg_chunk = nullptr;  // chunks of the per-instance reductions
   double *part = nullptr, *part2 = nullptr;
   double linear_rtol = -1.0;
+  int *dpos = nullptr;  // position of each row's diagonal in the CSR values
+  // strong-coupling clusters, rebuilt for every linear solve that uses them:
+  // label per cell, a change flag, local index in its cluster (-1: the cell
+  // takes its diagonal), the members of the 2..64-cell clusters (cluster by
+  // cluster, ascending cell index), their offsets and LU offsets, pivots
+  int *clab = nullptr, *cflag = nullptr, *cloc = nullptr, *cmem = nullptr, *coff = nullptr, *cpiv = nullptr;
+  long long *cluoff = nullptr;
+  int ncl = 0;  // clusters of 2..64 cells in the current solve
+  int precond_used = 0;
+  std::vector<int> h_lab, h_cnt, h_id, h_fill, h_loc, h_mem, h_off;
+  std::vector<long long> h_luoff;
   Krylov k32, k64;
   std::vector<void *> allocs;
   ~SolverState() {
-    for (Krylov *k : {&k32, &k64})
+    for (Krylov *k : {&k32, &k64}) {
       if (k->graph) cudaGraphExecDestroy(k->graph);
+      if (k->clu) cudaFree(k->clu);
+    }
     for (void *p : allocs) cudaFree(p);
   }
 };
@@ -328,6 +345,172 @@ __global__ void commit_kernel(int n, const int *cs, const int *commit, const dou
 }
 
 // ---------------------------------------------------------------------------
+// Strong-coupling clusters.  A coupling with |a_ij| >= tau sqrt(|a_ii a_jj|)
+// joins cells i and j; the connected clusters are found by label
+// propagation (every strong coupling hooks the labels of both cells to the
+// smaller one, then labels jump to their label's label).  The labels
+// converge to each cluster's smallest cell index whatever the order of the
+// atomic updates, so the clusters are deterministic.
+
+__global__ void cl_init_kernel(int n, int *lab) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) lab[i] = i;
+}
+
+__global__ void cl_hook_kernel(int n, const int *rowptr, const int *colidx, const int *dpos, const double *J,
+                               double tau, int *lab, int *flag) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double di = fabs(J[dpos[i]]);
+  for (int k = rowptr[i]; k < rowptr[i + 1]; k++) {
+    const int j = colidx[k];
+    if (j == i) continue;
+    const double aij = fabs(J[k]);
+    if (!(aij > 0.0) || !(aij >= tau * sqrt(di * fabs(J[dpos[j]])))) continue;
+    const int li = lab[i], lj = lab[j];
+    if (li != lj) {
+      const int m = li < lj ? li : lj;
+      atomicMin(&lab[li], m);
+      atomicMin(&lab[lj], m);
+      *flag = 1;
+    }
+  }
+}
+
+__global__ void cl_jump_kernel(int n, int *lab, int *flag) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int l = lab[i], ll = lab[l];
+  if (ll != l) {
+    lab[i] = ll;
+    *flag = 1;
+  }
+}
+
+// cells outside the 2..64-cell clusters precondition with their diagonal
+template <class T>
+__global__ void cl_diag_kernel(int n, const int *loc, const int *dpos, const double *J, T *inv) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || loc[i] >= 0) return;
+  const double d = J[dpos[i]];
+  inv[i] = d != 0.0 ? (T)(1.0 / d) : (T)1;
+}
+
+constexpr int kClusterMax = 64;
+constexpr int kClusterLd = kClusterMax + 1;  // padded row of the staged block
+
+// One warp per cluster: stage the cluster's block of J (every coupling
+// between its cells) in shared memory, factor it by LU with partial pivoting
+// (ties to the smaller row; a zero pivot becomes 1), store the factors.
+template <class T>
+__global__ void __launch_bounds__(32) cl_factor_kernel(int ncl, const int *coff, const long long *luoff,
+                                                       const int *cmem, const int *loc, const int *lab,
+                                                       const int *rowptr, const int *colidx, const double *J, T *lu,
+                                                       int *piv) {
+  extern __shared__ unsigned char cl_smem[];
+  T *B = reinterpret_cast<T *>(cl_smem);  // [kClusterMax][kClusterLd]
+  const int cl = blockIdx.x, lane = threadIdx.x;
+  if (cl >= ncl) return;
+  const int c0 = coff[cl], sz = coff[cl + 1] - c0;
+  for (int e = lane; e < sz * kClusterLd; e += 32) B[e] = (T)0;
+  __syncwarp();
+  for (int r = lane; r < sz; r += 32) {
+    const int m = cmem[c0 + r], L = lab[m];
+    for (int k = rowptr[m]; k < rowptr[m + 1]; k++) {
+      const int col = colidx[k];
+      if (lab[col] == L) B[r * kClusterLd + loc[col]] = (T)J[k];
+    }
+  }
+  __syncwarp();
+  for (int kk = 0; kk < sz; kk++) {
+    T best = (T)-1;
+    int bi = kk;
+    for (int i = kk + lane; i < sz; i += 32) {
+      const T v = B[i * kClusterLd + kk] < (T)0 ? -B[i * kClusterLd + kk] : B[i * kClusterLd + kk];
+      if (v > best) {
+        best = v;
+        bi = i;
+      }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const T ob = __shfl_down_sync(0xffffffffu, best, off);
+      const int oi = __shfl_down_sync(0xffffffffu, bi, off);
+      if (ob > best || (ob == best && oi < bi)) {
+        best = ob;
+        bi = oi;
+      }
+    }
+    bi = __shfl_sync(0xffffffffu, bi, 0);
+    if (lane == 0) piv[c0 + kk] = bi;
+    if (bi != kk)
+      for (int j = lane; j < sz; j += 32) {
+        const T t = B[kk * kClusterLd + j];
+        B[kk * kClusterLd + j] = B[bi * kClusterLd + j];
+        B[bi * kClusterLd + j] = t;
+      }
+    __syncwarp();
+    T pv = B[kk * kClusterLd + kk];
+    if (pv == (T)0) pv = (T)1;
+    __syncwarp();
+    if (lane == 0) B[kk * kClusterLd + kk] = pv;
+    for (int i = kk + 1 + lane; i < sz; i += 32) {
+      const T l = B[i * kClusterLd + kk] / pv;
+      B[i * kClusterLd + kk] = l;
+      for (int j = kk + 1; j < sz; j++) B[i * kClusterLd + j] -= l * B[kk * kClusterLd + j];
+    }
+    __syncwarp();
+  }
+  T *out = lu + luoff[cl];
+  for (int e = lane; e < sz * sz; e += 32) out[e] = B[(e / sz) * kClusterLd + e % sz];
+}
+
+template <class T>
+__global__ void cl_apply_diag_kernel(int n, const int *loc, const T *inv, const T *in, T *out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && loc[i] < 0) out[i] = inv[i] * in[i];
+}
+
+// out = (cluster block)^-1 in, one warp per cluster: the row swaps, then the
+// unit-lower and upper triangular solves
+template <class T>
+__global__ void __launch_bounds__(32) cl_apply_kernel(int ncl, const int *coff, const long long *luoff,
+                                                      const int *cmem, const T *lu, const int *piv, const T *in,
+                                                      T *out) {
+  __shared__ T x[kClusterMax];
+  const int cl = blockIdx.x, lane = threadIdx.x;
+  if (cl >= ncl) return;
+  const int c0 = coff[cl], sz = coff[cl + 1] - c0;
+  for (int r = lane; r < sz; r += 32) x[r] = in[cmem[c0 + r]];
+  __syncwarp();
+  if (lane == 0)
+    for (int kk = 0; kk < sz; kk++) {
+      const int p = piv[c0 + kk];
+      if (p != kk) {
+        const T t = x[kk];
+        x[kk] = x[p];
+        x[p] = t;
+      }
+    }
+  __syncwarp();
+  const T *L = lu + luoff[cl];
+  for (int kk = 0; kk < sz; kk++) {
+    const T xk = x[kk];
+    __syncwarp();
+    for (int i = kk + 1 + lane; i < sz; i += 32) x[i] -= L[i * sz + kk] * xk;
+    __syncwarp();
+  }
+  for (int kk = sz - 1; kk >= 0; kk--) {
+    if (lane == 0) x[kk] /= L[kk * sz + kk];
+    __syncwarp();
+    const T xk = x[kk];
+    for (int i = lane; i < kk; i += 32) x[i] -= L[i * sz + kk] * xk;
+    __syncwarp();
+  }
+  for (int r = lane; r < sz; r += 32) out[cmem[c0 + r]] = x[r];
+}
+
+// ---------------------------------------------------------------------------
 template <class T>
 int spmv(SolverState *s, const Krylov &k, const T *x, T *y, cudaStream_t st) {
   const T *A = (const T *)k.Jv;
@@ -360,25 +543,39 @@ int dot(SolverState *s, const T *a, const T *b, const T *c, const T *d, int slot
   return 0;
 }
 
+// out = M^-1 in with the preconditioner of the current solve
+template <class T>
+void precondition(SolverState *s, Krylov &k, const T *in, T *out, cudaStream_t st) {
+  if (s->precond_used == TDY_PRECOND_CLUSTERS) {
+    cl_apply_diag_kernel<T><<<nblk(s->n, 256), 256, 0, st>>>(s->n, s->cloc, (const T *)k.cinv, in, out);
+    if (s->ncl > 0)
+      cl_apply_kernel<T><<<s->ncl, 32, 0, st>>>(s->ncl, s->coff, s->cluoff, s->cmem, (const T *)k.clu, s->cpiv, in,
+                                                out);
+  } else {
+    line_solve_kernel<T><<<nblk(s->nlines, 128), 128, 0, st>>>(s->nlines, s->line_off, s->line_cells,
+                                                                (const T *)k.la, (const T *)k.lcp, (const T *)k.linv,
+                                                                in, out);
+  }
+}
+
 // one BiCGStab iteration for every active instance (the graph body)
 template <class T>
 void bicgstab_iteration(SolverState *s, Krylov &k, double tol2, cudaStream_t st) {
   const int n = s->n, ns = s->nseg;
-  const unsigned gb = nblk(n, 256), sb = nblk(ns, 128), lb = nblk(s->nlines, 128);
+  const unsigned gb = nblk(n, 256), sb = nblk(ns, 128);
   T *r = (T *)k.r, *r0 = (T *)k.r0, *p = (T *)k.p, *v = (T *)k.v, *sv = (T *)k.s, *tv = (T *)k.t;
   T *ph = (T *)k.ph, *sh = (T *)k.sh, *y = (T *)k.y;
-  const T *la = (const T *)k.la, *lcp = (const T *)k.lcp, *linv = (const T *)k.linv;
   dot<T>(s, r0, r, nullptr, nullptr, S_T1, 0, st);
   scal_beta_kernel<<<sb, 128, 0, st>>>(ns, s->lin_active, s->scal);
   p_update_kernel<T><<<gb, 256, 0, st>>>(n, s->cell_seg, s->lin_active, s->scal, ns, r, v, p);
-  line_solve_kernel<T><<<lb, 128, 0, st>>>(s->nlines, s->line_off, s->line_cells, la, lcp, linv, p, ph);
+  precondition<T>(s, k, p, ph, st);
   spmv<T>(s, k, ph, v, st);
   dot<T>(s, r0, v, nullptr, nullptr, S_T1, 0, st);
   scal_alpha_kernel<<<sb, 128, 0, st>>>(ns, s->lin_active, s->scal);
   s_update_kernel<T><<<gb, 256, 0, st>>>(n, s->cell_seg, s->lin_active, s->scal, ns, r, v, sv);
   dot<T>(s, sv, sv, nullptr, nullptr, S_T1, 0, st);
   scal_half_kernel<<<sb, 128, 0, st>>>(ns, s->lin_active, s->scal, tol2);
-  line_solve_kernel<T><<<lb, 128, 0, st>>>(s->nlines, s->line_off, s->line_cells, la, lcp, linv, sv, sh);
+  precondition<T>(s, k, sv, sh, st);
   spmv<T>(s, k, sh, tv, st);
   dot<T>(s, tv, tv, tv, sv, S_T1, S_T2, st);
   scal_omega_kernel<<<sb, 128, 0, st>>>(ns, s->lin_active, s->scal);
@@ -445,6 +642,105 @@ int autotune_spmv(SolverState *s, Krylov &k, cudaStream_t st) {
   return 0;
 }
 
+// Clusters for the current Jacobian: label propagation on the device (at
+// most kClusterRounds rounds of one hook pass and four jump passes, until a
+// round changes nothing), compaction on the host in cell order, then the
+// factors.  Returns 0 with precond_used = TDY_PRECOND_LINES when the labels
+// have not settled (the caller then factors the lines).
+constexpr int kClusterRounds = 64;
+
+template <class T>
+int cluster_setup(SolverState *s, Krylov &k, double tau, cudaStream_t st) {
+  int ierr;
+  const int n = s->n;
+  if (!s->clab) {
+    if ((ierr = salloc(s, &s->clab, n))) return ierr;
+    if ((ierr = salloc(s, &s->cflag, 1))) return ierr;
+    if ((ierr = salloc(s, &s->cloc, n))) return ierr;
+    if ((ierr = salloc(s, &s->cmem, n))) return ierr;
+    if ((ierr = salloc(s, &s->coff, n + 1))) return ierr;
+    if ((ierr = salloc(s, &s->cluoff, n + 1))) return ierr;
+    if ((ierr = salloc(s, &s->cpiv, n))) return ierr;
+  }
+  if (!k.cinv) {
+    T *p;
+    if ((ierr = salloc(s, &p, n))) return ierr;
+    k.cinv = p;
+  }
+  cl_init_kernel<<<nblk(n, 256), 256, 0, st>>>(n, s->clab);
+  bool settled = false;
+  for (int round = 0; round < kClusterRounds && !settled; round++) {
+    SCUDA(cudaMemsetAsync(s->cflag, 0, sizeof(int), st));
+    cl_hook_kernel<<<nblk(n, 128), 128, 0, st>>>(n, s->rowptr, s->colidx, s->dpos, s->J, tau, s->clab, s->cflag);
+    for (int j = 0; j < 4; j++) cl_jump_kernel<<<nblk(n, 256), 256, 0, st>>>(n, s->clab, s->cflag);
+    int flag = 1;
+    SCUDA(cudaMemcpyAsync(&flag, s->cflag, sizeof(int), cudaMemcpyDeviceToHost, st));
+    SCUDA(cudaStreamSynchronize(st));
+    settled = flag == 0;
+  }
+  if (!settled) {
+    s->precond_used = TDY_PRECOND_LINES;
+    return 0;
+  }
+  // compaction: clusters of 2..kClusterMax cells in order of their smallest
+  // cell, members in ascending cell order
+  std::vector<int> &lab = s->h_lab, &cnt = s->h_cnt, &id = s->h_id, &fill = s->h_fill, &loc = s->h_loc,
+                   &mem = s->h_mem, &off = s->h_off;
+  std::vector<long long> &luoff = s->h_luoff;
+  lab.resize(n);
+  SCUDA(cudaMemcpyAsync(lab.data(), s->clab, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
+  SCUDA(cudaStreamSynchronize(st));
+  cnt.assign(n, 0);
+  for (int i = 0; i < n; i++) {
+    if (lab[i] < 0 || lab[i] >= n) return set_error(TDY_ERR_LIB, "solver: cluster label %d out of range", lab[i]);
+    cnt[lab[i]]++;
+  }
+  id.assign(n, -1);
+  off.assign(1, 0);
+  luoff.assign(1, 0);
+  int ncl = 0;
+  for (int r = 0; r < n; r++)
+    if (cnt[r] >= 2 && cnt[r] <= kClusterMax) {
+      id[r] = ncl++;
+      off.push_back(off.back() + cnt[r]);
+      luoff.push_back(luoff.back() + (long long)cnt[r] * cnt[r]);
+    }
+  fill.assign(ncl, 0);
+  loc.assign(n, -1);
+  mem.resize(off.back());
+  for (int i = 0; i < n; i++) {
+    const int c = id[lab[i]];
+    if (c < 0) continue;
+    loc[i] = fill[c]++;
+    mem[off[c] + loc[i]] = i;
+  }
+  s->ncl = ncl;
+  SCUDA(cudaMemcpyAsync(s->cloc, loc.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st));
+  if (ncl > 0) {
+    SCUDA(cudaMemcpyAsync(s->cmem, mem.data(), sizeof(int) * mem.size(), cudaMemcpyHostToDevice, st));
+    SCUDA(cudaMemcpyAsync(s->coff, off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice, st));
+    SCUDA(cudaMemcpyAsync(s->cluoff, luoff.data(), sizeof(long long) * luoff.size(), cudaMemcpyHostToDevice, st));
+    const size_t need = (size_t)luoff.back();
+    if (need > k.clu_cap) {
+      SCUDA(cudaStreamSynchronize(st));
+      if (k.clu) cudaFree(k.clu);
+      k.clu = nullptr;
+      k.clu_cap = 0;
+      SCUDA(cudaMalloc(&k.clu, need * sizeof(T)));
+      k.clu_cap = need;
+    }
+  }
+  cl_diag_kernel<T><<<nblk(n, 256), 256, 0, st>>>(n, s->cloc, s->dpos, s->J, (T *)k.cinv);
+  if (ncl > 0)
+    cl_factor_kernel<T><<<ncl, 32, kClusterMax * kClusterLd * sizeof(T), st>>>(
+        ncl, s->coff, s->cluoff, s->cmem, s->cloc, s->clab, s->rowptr, s->colidx, s->J, (T *)k.clu, s->cpiv);
+  SCUDA(cudaGetLastError());
+  // the host vectors above stay alive until the copies complete
+  SCUDA(cudaStreamSynchronize(st));
+  s->precond_used = TDY_PRECOND_CLUSTERS;
+  return 0;
+}
+
 template <class T>
 int linear_solve(SolverState *s, Krylov &k, const TDyNewtonOptions &o, cudaStream_t st, long long *lin_total,
                  std::vector<int> &inst_lin_its) {
@@ -453,8 +749,11 @@ int linear_solve(SolverState *s, Krylov &k, const TDyNewtonOptions &o, cudaStrea
   if ((ierr = autotune_spmv<T>(s, k, st))) return ierr;  // uses b and v as scratch before they are set
   const int n = s->n, ns = s->nseg;
   cast_kernel<T><<<nblk(s->nnz, 256), 256, 0, st>>>(s->nnz, s->J, (T *)k.Jv);
-  line_factor_kernel<T><<<nblk(s->nlines, 128), 128, 0, st>>>(s->nlines, s->line_off, s->pos_d, s->pos_lo, s->pos_hi,
-                                                               s->J, (T *)k.la, (T *)k.lcp, (T *)k.linv);
+  s->precond_used = TDY_PRECOND_LINES;
+  if (o.precond == TDY_PRECOND_CLUSTERS && (ierr = cluster_setup<T>(s, k, o.cluster_threshold, st))) return ierr;
+  if (s->precond_used == TDY_PRECOND_LINES)
+    line_factor_kernel<T><<<nblk(s->nlines, 128), 128, 0, st>>>(s->nlines, s->line_off, s->pos_d, s->pos_lo,
+                                                                 s->pos_hi, s->J, (T *)k.la, (T *)k.lcp, (T *)k.linv);
   init_kernel<T><<<nblk(n, 256), 256, 0, st>>>(n, s->cell_seg, s->newt_active, s->F, (T *)k.b, (T *)k.r, (T *)k.r0,
                                                (T *)k.p, (T *)k.v, (T *)k.y);
   dot<T>(s, (T *)k.b, (T *)k.b, nullptr, nullptr, S_BNORM2, 0, st);
@@ -462,7 +761,9 @@ int linear_solve(SolverState *s, Krylov &k, const TDyNewtonOptions &o, cudaStrea
   init_scalars_kernel<<<nblk(ns, 128), 128, 0, st>>>(ns, s->newt_active, s->lin_active, s->lin_its, s->scal);
   SCUDA(cudaGetLastError());
   const double tol2 = o.linear_rtol * o.linear_rtol;
-  if (!k.graph || k.graph_stream != st || s->linear_rtol != o.linear_rtol) {
+  // the cluster launches depend on this solve's cluster count: recapture
+  if (!k.graph || k.graph_stream != st || s->linear_rtol != o.linear_rtol || k.graph_precond != s->precond_used ||
+      s->precond_used == TDY_PRECOND_CLUSTERS) {
     if (k.graph) cudaGraphExecDestroy(k.graph);
     k.graph = nullptr;
     cudaGraph_t g;
@@ -473,6 +774,7 @@ int linear_solve(SolverState *s, Krylov &k, const TDyNewtonOptions &o, cudaStrea
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return set_error(TDY_ERR_GPU, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
     k.graph_stream = st;
+    k.graph_precond = s->precond_used;
     s->linear_rtol = o.linear_rtol;
   }
   std::vector<int> act(ns), its(ns);
@@ -547,6 +849,11 @@ int solver_init(_p_TDy *t) {
   if ((ierr = sup(s, &s->line_off, line_off))) return ierr;
   if ((ierr = sup(s, &s->line_cells, line_cells))) return ierr;
   if ((ierr = sup(s, &s->pos_d, pd))) return ierr;
+  {
+    std::vector<int> dp(s->n);
+    for (int i = 0; i < s->n; i++) dp[i] = find(i, i);  // every row has its diagonal (checked above per line cell)
+    if ((ierr = sup(s, &s->dpos, dp))) return ierr;
+  }
   if ((ierr = sup(s, &s->pos_lo, plo))) return ierr;
   if ((ierr = sup(s, &s->pos_hi, phi))) return ierr;
   if ((ierr = salloc(s, &s->x, s->n))) return ierr;
