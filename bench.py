@@ -323,7 +323,8 @@ def batched_config4(ninst=4096, sample=64, dt=3600.0):
     }
 
 
-def prisms_config3(ntri=20000, nlayers=40, steps=20, dt=20.0, rotation="vertical", oracle_every_step_max_cells=4_000_000):
+def prisms_config3(ntri=20000, nlayers=40, steps=20, dt=20.0, rotation="vertical", oracle_every_step_max_cells=4_000_000,
+                   precond="lines"):
     """Config 3: infiltration (1e-7 m/s through the top) into a dry soil on
     Delaunay triangular prisms with per-cell full-tensor K, advanced ``steps``
     backward-Euler steps of ``dt`` by the device Newton in the mixed form
@@ -358,7 +359,7 @@ def prisms_config3(ntri=20000, nlayers=40, steps=20, dt=20.0, rotation="vertical
     # warm-up: spmv autotune and graph capture of both arithmetic modes
     for fp32 in (True, False):
         w = d.clone()
-        t.backward_euler_step_device(w, dt, fp32=fp32)
+        t.backward_euler_step_device(w, dt, fp32=fp32, precond=precond)
     del w
     every = nc <= oracle_every_step_max_cells
     per_step, mixed_s, fp64_s = [], 0.0, 0.0
@@ -367,11 +368,11 @@ def prisms_config3(ntri=20000, nlayers=40, steps=20, dt=20.0, rotation="vertical
         d64 = d.clone()
         torch.cuda.synchronize()
         ts = time.perf_counter()
-        st, its, rel = t.backward_euler_step_device(d, dt, fp32=True)
+        st, its, rel = t.backward_euler_step_device(d, dt, fp32=True, precond=precond)
         torch.cuda.synchronize()
         tm = time.perf_counter() - ts
         ts = time.perf_counter()
-        st64, its64, rel64 = t.backward_euler_step_device(d64, dt, fp32=False)
+        st64, its64, rel64 = t.backward_euler_step_device(d64, dt, fp32=False, precond=precond)
         torch.cuda.synchronize()
         td = time.perf_counter() - ts
         mixed_s += tm
@@ -397,7 +398,7 @@ def prisms_config3(ntri=20000, nlayers=40, steps=20, dt=20.0, rotation="vertical
     checked = [r for r in per_step if "oracle_rel_residual" in r]
     return {
         "workload": info["workload"], "ncells": nc, "nnz_jacobian": nnz,
-        "rotation": info["rotation"], "van_genuchten": info["van_genuchten"],
+        "rotation": info["rotation"], "van_genuchten": info["van_genuchten"], "preconditioner": precond,
         "initial_pressure_pa": info["initial_pressure_pa"], "depth_m": info["depth_m"],
         "top_flux_m_per_s": info["top_flux_m_per_s"], "dt_s": dt, "steps": steps, "setup_s": setup_s,
         "mixed_s_total": mixed_s, "fp64_s_total": fp64_s, "speedup_mixed_vs_fp64": fp64_s / mixed_s,
@@ -735,7 +736,7 @@ def run_gpu(args, rank, world, local_rank):
         cfg3 = None
         if args.prisms_triangles > 0:
             try:
-                cfg3 = prisms_config3(args.prisms_triangles, dt=args.prisms_dt)
+                cfg3 = prisms_config3(args.prisms_triangles, dt=args.prisms_dt, precond=args.prisms_precond)
             except Exception as e:
                 cfg3 = {"error": repr(e)}
         if args.prisms_eval_triangles > 0:
@@ -812,6 +813,8 @@ def main():
                     help="surface triangles of the prism infiltration measurement (0 skips it)")
     ap.add_argument("--prisms-dt", type=float, default=20.0,
                     help="time step of the prism infiltration measurement (s)")
+    ap.add_argument("--prisms-precond", default="lines", choices=["lines", "clusters"],
+                    help="inner-solve preconditioner of the prism infiltration measurement")
     ap.add_argument("--prisms-eval-triangles", type=int, default=0,
                     help="surface triangles of the mixed-form F+J evaluation on prisms with 3-D rotated K "
                          "(200000 is the full configuration; 0 skips it)")
