@@ -239,9 +239,15 @@ typedef struct {
 typedef struct {
   int newton_iterations;        /* largest over the instances */
   long long linear_iterations;  /* BiCGStab iterations, summed over instances and Newton iterations */
-  int converged;                /* instances that met the tolerance */
+  int converged;                /* instances whose FP64 residual met rtol (or atol) */
   int ninstances;
   double max_rel_residual;      /* largest final ||F|| / ||F_0|| */
+  int step_converged;           /* instances ended by the step test (stol) above rtol: not in `converged` */
+  int precond_used;             /* preconditioner of the last inner solve (TDY_PRECOND_*); CLUSTERS falls
+                                   back to LINES when the cluster labels do not settle */
+  int clusters;                 /* last inner solve: clusters of 2..64 cells factored */
+  int cluster_cells;            /* last inner solve: cells in those clusters */
+  int cluster_cells_diagonal;   /* last inner solve: cells of clusters larger than 64 (they take their diagonal) */
 } TDyNewtonStats;
 TDyErrorCode TDyNewtonOptionsDefault(TDyNewtonOptions *o);
 TDyErrorCode TDyGetNumInstances(TDy tdy, int *n);

@@ -76,7 +76,9 @@ PRECOND_LINES, PRECOND_CLUSTERS = 0, 1
 
 class NewtonStats(ctypes.Structure):
     _fields_ = [("newton_iterations", c_int), ("linear_iterations", c_longlong), ("converged", c_int),
-                ("ninstances", c_int), ("max_rel_residual", c_double)]
+                ("ninstances", c_int), ("max_rel_residual", c_double), ("step_converged", c_int),
+                ("precond_used", c_int), ("clusters", c_int), ("cluster_cells", c_int),
+                ("cluster_cells_diagonal", c_int)]
 
 
 def _sig(name, *args):

@@ -9,6 +9,15 @@ namespace tdy {
 // as transient variable (M_t given)
 enum { FORM_SNES = 0, FORM_TS = 1, FORM_TV = 2 };
 
+// Device memory of handles and their solvers: stream-ordered allocation
+// (cudaMallocAsync / cudaFreeAsync from the device's default pool) on the
+// handle's stream, so that setting up or destroying a handle never
+// synchronises the device and handles served by other threads keep running.
+// A pointer from dmem_alloc is usable on other streams once `stream` has
+// been synchronised.
+int dmem_alloc(void **p, size_t bytes, void *stream);
+void dmem_free(void *p, void *stream);
+
 int device_setup(_p_TDy *t);
 void device_destroy(_p_TDy *t);
 int device_upload_source_sink(_p_TDy *t);
@@ -39,6 +48,6 @@ int device_be_solve(_p_TDy *t, double dt, double *dU, const TDyNewtonOptions &o,
 void device_solver_destroy(_p_TDy *t);
 int device_num_instances(_p_TDy *t);
 // Trans of the canonical vertices into d_Tc (-tdy_mpfao_setup_on_device).
-int device_canon_trans(const _p_TDy *t, const int *d_cellc, const int *d_facec, double *d_Tc);
+int device_canon_trans(const _p_TDy *t, const int *d_cellc, const int *d_facec, double *d_Tc, void *stream);
 
 }  // namespace tdy

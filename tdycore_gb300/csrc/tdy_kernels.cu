@@ -135,6 +135,14 @@ struct DeviceState {
   std::vector<Slab> slabs;
   cudaStream_t copy_stream = nullptr;
   std::vector<cudaEvent_t> slab_ev;
+  // callers' streams that enqueued work on this handle, each with an event
+  // recorded after its last enqueue: TDyDestroy waits for them before the
+  // stream-ordered frees (which do not synchronise the device)
+  std::vector<std::pair<cudaStream_t, cudaEvent_t>> user_streams;
+  // recorded after every allocation-free evaluation (created at set-up, so
+  // that call creates nothing); such calls never overlap, so the last one
+  // covers them all
+  cudaEvent_t noalloc_ev = nullptr;
 };
 
 #define CUDA_TRY(call)                                                                          \
@@ -968,21 +976,69 @@ __global__ void __launch_bounds__(32 * kCellWarps) generic_cell_kernel(DevArgs a
 // ---------------------------------------------------------------------------
 // Host side
 
+// Stream-ordered device memory; the pool keeps up to kPoolKeep bytes of
+// freed memory for reuse instead of returning it to the driver at every
+// synchronisation (a server sets up and destroys handles continuously).
+static constexpr unsigned long long kPoolKeep = 8ull << 30;
+static constexpr int kMaxDevices = 64;
+static std::mutex g_dev_mutex;  // per-device one-time set-up below
+static bool g_pool_set[kMaxDevices] = {};
+
+int dmem_alloc(void **p, size_t bytes, void *stream) {
+  *p = nullptr;
+  int dev = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  if (dev >= 0 && dev < kMaxDevices) {
+    std::lock_guard<std::mutex> lk(g_dev_mutex);
+    if (!g_pool_set[dev]) {
+      cudaMemPool_t pool;
+      CUDA_TRY(cudaDeviceGetDefaultMemPool(&pool, dev));
+      unsigned long long keep = kPoolKeep;
+      CUDA_TRY(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+      g_pool_set[dev] = true;
+    }
+  }
+  cudaError_t e = cudaMallocAsync(p, bytes ? bytes : 1, (cudaStream_t)stream);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    return set_error(TDY_ERR_GPU, "cudaMallocAsync(%zu bytes): %s", bytes, cudaGetErrorString(e));
+  }
+  return 0;
+}
+
+void dmem_free(void *p, void *stream) {
+  if (p) cudaFreeAsync(p, (cudaStream_t)stream);
+}
+
 template <class T>
 static int dalloc(DeviceState *d, T **p, size_t n) {
-  *p = nullptr;
-  if (n == 0) n = 1;
-  cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
-  if (e != cudaSuccess) return set_error(TDY_ERR_GPU, "cudaMalloc(%zu bytes): %s", n * sizeof(T), cudaGetErrorString(e));
+  int ierr = dmem_alloc((void **)p, (n ? n : 1) * sizeof(T), d->stream);
+  if (ierr) return ierr;
   d->allocs.push_back(*p);
   return 0;
 }
 
+// (h must stay alive until d->stream is synchronised)
 template <class T>
 static int dupload(DeviceState *d, T **p, const std::vector<T> &h) {
   int ierr = dalloc(d, p, h.size());
   if (ierr) return ierr;
-  if (!h.empty()) CUDA_TRY(cudaMemcpy(*p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+  if (!h.empty()) CUDA_TRY(cudaMemcpyAsync(*p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, d->stream));
+  return 0;
+}
+
+// Records that a caller's stream enqueued work on this handle.
+static int note_stream(DeviceState *d, cudaStream_t st) {
+  if (st == d->stream) return 0;
+  for (auto &u : d->user_streams)
+    if (u.first == st) {
+      CUDA_TRY(cudaEventRecord(u.second, st));
+      return 0;
+    }
+  cudaEvent_t e;
+  CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  d->user_streams.emplace_back(st, e);
+  CUDA_TRY(cudaEventRecord(e, st));
   return 0;
 }
 
@@ -1037,6 +1093,24 @@ static void build_slabs(_p_TDy *t, DeviceState *d) {
     sl.j1 = s.rowptr[cut[k + 1]];
     d->slabs.push_back(sl);
   }
+}
+
+static int noalloc_resolve(int dev);
+static size_t cell_smem_bytes(const DevArgs &a, bool gen_warp);
+static bool cell_warp_form(const DevArgs &a);
+
+// Dynamic shared memory above 48 KB is an opt-in per kernel and device; it
+// is made at set-up with the device current (and only ever raised).
+static size_t g_cell_smem_granted[kMaxDevices] = {};
+static int cell_smem_optin(int dev, size_t bytes) {
+  if (bytes <= 48 * 1024) return 0;
+  if (dev < 0 || dev >= kMaxDevices) return set_error(TDY_ERR_SUP, "device ordinal %d not supported", dev);
+  std::lock_guard<std::mutex> lk(g_dev_mutex);
+  if (bytes > g_cell_smem_granted[dev]) {
+    CUDA_TRY(cudaFuncSetAttribute(cell_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    g_cell_smem_granted[dev] = bytes;
+  }
+  return 0;
 }
 
 int device_setup(_p_TDy *t) {
@@ -1113,7 +1187,8 @@ int device_setup(_p_TDy *t) {
   a.jac_ff = t->opt.jacobian_arithmetic == JACOBIAN_DOUBLE_FLOAT;
   UP(a.cellc, s.cellc);
   UP(a.facec, s.facec);
-  if (t->opt.setup_on_device && (ierr = device_canon_trans(t, a.cellc, a.facec, const_cast<double *>(a.Tc))))
+  if (t->opt.setup_on_device &&
+      (ierr = device_canon_trans(t, a.cellc, a.facec, const_cast<double *>(a.Tc), d->stream)))
     return ierr;
   a.ngen = (int)s.gen_vertex.size();
   // per row: w, E_up, E_dn, flux (doubles) and the two local-cell indices
@@ -1158,7 +1233,7 @@ int device_setup(_p_TDy *t) {
   if ((ierr = dalloc(d, &a.acc_b, m.nc))) return ierr;
   if ((ierr = dalloc(d, &a.jdiag, m.nc))) return ierr;
   if ((ierr = dalloc(d, &p, m.nc))) return ierr;
-  CUDA_TRY(cudaMemset(p, 0, sizeof(double) * m.nc));
+  CUDA_TRY(cudaMemsetAsync(p, 0, sizeof(double) * m.nc, d->stream));
   a.accum_prev = p;
   if ((ierr = dalloc(d, &a.scratch, (size_t)s.scratch_size))) return ierr;
   d->nnz = (int)s.colidx.size();
@@ -1174,14 +1249,30 @@ int device_setup(_p_TDy *t) {
     d->slab_ev.assign(d->slabs.size(), nullptr);
     for (cudaEvent_t &e : d->slab_ev) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   }
-  CUDA_TRY(cudaDeviceSynchronize());
+  if ((ierr = cell_smem_optin(d->device, cell_smem_bytes(a, cell_warp_form(a))))) return ierr;
+  if ((ierr = noalloc_resolve(d->device))) return ierr;
+  CUDA_TRY(cudaEventCreateWithFlags(&d->noalloc_ev, cudaEventDisableTiming));
+  // the uploads (and the device-built Trans) are complete before any other
+  // stream uses them; only this handle's stream is waited for
+  CUDA_TRY(cudaStreamSynchronize(d->stream));
   return 0;
 }
 
+// Waits for the work this handle has in flight (its own streams and the
+// callers' streams it has seen), then frees its memory stream-ordered: no
+// device-wide synchronisation, so other handles keep running.
 void device_destroy(_p_TDy *t) {
   DeviceState *d = t->dev;
   if (!d) return;
   if (d->stream) cudaStreamSynchronize(d->stream);
+  for (auto &u : d->user_streams) {
+    cudaEventSynchronize(u.second);
+    cudaEventDestroy(u.second);
+  }
+  if (d->noalloc_ev) {
+    cudaEventSynchronize(d->noalloc_ev);
+    cudaEventDestroy(d->noalloc_ev);
+  }
   for (int k = 0; k < 4; k++)
     if (d->ev[k]) cudaEventDestroy(d->ev[k]);
   if (d->copy_stream) {
@@ -1189,16 +1280,20 @@ void device_destroy(_p_TDy *t) {
     cudaStreamDestroy(d->copy_stream);
   }
   for (cudaEvent_t e : d->slab_ev) cudaEventDestroy(e);
-
-  for (void *p : d->allocs) cudaFree(p);
-  if (d->stream) cudaStreamDestroy(d->stream);
+  if (d->stream) {
+    for (void *p : d->allocs) dmem_free(p, d->stream);
+    cudaStreamSynchronize(d->stream);
+    cudaStreamDestroy(d->stream);
+  }
   delete d;
   t->dev = nullptr;
 }
 
 int device_upload_source_sink(_p_TDy *t) {
   DeviceState *d = t->dev;
-  CUDA_TRY(cudaMemcpy((void *)d->a.ss, t->mat.source_sink.data(), sizeof(double) * t->mesh.nc, cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpyAsync((void *)d->a.ss, t->mat.source_sink.data(), sizeof(double) * t->mesh.nc,
+                           cudaMemcpyHostToDevice, d->stream));
+  CUDA_TRY(cudaStreamSynchronize(d->stream));
   return 0;
 }
 
@@ -1228,7 +1323,7 @@ int device_presolve(_p_TDy *t, const double *dUprev, void *stream) {
   a.dt = t->dtime;
   presolve_kernel<<<nblocks(a.nc, 256), 256, 0, st>>>(a, dUprev, (double *)a.accum_prev);
   CUDA_TRY(cudaGetLastError());
-  return 0;
+  return note_stream(d, st);
 }
 
 int device_presolve_host(_p_TDy *t, const double *Uprev) {
@@ -1276,17 +1371,15 @@ static int launch_vertices(const DevArgs &a, bool gen_warp, cudaStream_t st) {
 
 // Cell stage over the cells a names (sc_cells/nS, gc_cells/ngc); gen_warp:
 // mostly other cells take the warp form.
+static size_t cell_smem_bytes(const DevArgs &a, bool gen_warp) {
+  return 64 * (size_t)(gen_warp || a.max_row_nnz < 27 ? 27 : a.max_row_nnz) * sizeof(double);
+}
+
+// (rows longer than 96 entries need more than 48 KB of dynamic shared
+// memory: device_setup opts in for the handle's device)
 static int launch_cells(const DevArgs &a, bool gen_warp, cudaStream_t st) {
-  const size_t cell_smem = 64 * (size_t)(gen_warp || a.max_row_nnz < 27 ? 27 : a.max_row_nnz) * sizeof(double);
+  const size_t cell_smem = cell_smem_bytes(a, gen_warp);
   const int sb = (int)nblocks(a.nS, 64), gcb = gen_warp ? 0 : (int)nblocks(a.ngc, 64);
-  if (cell_smem > 48 * 1024) {
-    // rows longer than 96 entries: opt in to more dynamic shared memory
-    static thread_local size_t granted = 48 * 1024;
-    if (cell_smem > granted) {
-      CUDA_TRY(cudaFuncSetAttribute(cell_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cell_smem));
-      granted = cell_smem;
-    }
-  }
   if (sb + gcb > 0) cell_kernel<<<sb + gcb, 64, cell_smem, st>>>(a, sb);
   if (gen_warp && a.ngc > 0) {
     const size_t gcell_smem = (size_t)2 * kCellWarps * (size_t)a.max_row_nnz * sizeof(double);
@@ -1343,6 +1436,7 @@ int device_eval(_p_TDy *t, int form, double time, const double *dU, const double
   if (ierr) return ierr;
   ierr = launch_eval(a, st, d->timers ? d->ev : nullptr);
   if (ierr) return ierr;
+  if ((ierr = note_stream(d, st))) return ierr;
   if (d->timers) {
     CUDA_TRY(cudaEventSynchronize(d->ev[3]));
     for (int k = 0; k < 3; k++) {
@@ -1528,18 +1622,28 @@ int device_eval_host(_p_TDy *t, int form, double time, const double *U, const do
 // memory.  The array is 64 MiB of doubles; every GPU that loads the library
 // holds it until the process exits.  Host code never uses the array's name as
 // an address (on the host it is only a stand-in for the symbol): the device
-// address is looked up once per device with cudaGetSymbolAddress while that
-// device is current, on the first call made on it.
+// address is looked up with cudaGetSymbolAddress once per device, while that
+// device is current, by TDySetup (noalloc_resolve), so the call itself loads
+// no module and allocates nothing, even the first time.
 //
 // All calls share the array and it keeps the last call's contents.  Nothing
 // has to start at zero: vertex_kernel writes every partial that cell_kernel
 // then reads in the same call.  Calls that overlap on the GPU (two streams, or
 // two handles at once) race on the array and must be serialised by the caller.
 #define TDY_NOALLOC_SCRATCH_DOUBLES (8ull << 20)
-#define TDY_NOALLOC_MAX_DEVICES 64
 static __device__ __align__(256) double g_noalloc_scratch[TDY_NOALLOC_SCRATCH_DOUBLES];
-static double *g_noalloc_ptr[TDY_NOALLOC_MAX_DEVICES] = {};
-static std::mutex g_noalloc_mutex;
+static double *g_noalloc_ptr[kMaxDevices] = {};
+
+static int noalloc_resolve(int dev) {
+  if (dev < 0 || dev >= kMaxDevices) return set_error(TDY_ERR_SUP, "device ordinal %d not supported", dev);
+  std::lock_guard<std::mutex> lk(g_dev_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void *p = nullptr;
+    CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    g_noalloc_ptr[dev] = (double *)p;
+  }
+  return 0;
+}
 
 int device_eval_noalloc(_p_TDy *t, const double *dU, double *dR, double *dJ, void *stream) {
   DeviceState *d = t->dev;
@@ -1555,17 +1659,12 @@ int device_eval_noalloc(_p_TDy *t, const double *dU, double *dR, double *dJ, voi
   if (dev != d->device)
     return set_error(TDY_ERR_USER, "current CUDA device %d is not the device %d this handle was set up on", dev,
                      d->device);
-  if (dev < 0 || dev >= TDY_NOALLOC_MAX_DEVICES) return set_error(TDY_ERR_SUP, "device ordinal %d not supported", dev);
   double *scratch = nullptr;
   {
-    std::lock_guard<std::mutex> lk(g_noalloc_mutex);
-    if (!g_noalloc_ptr[dev]) {
-      void *p = nullptr;
-      CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-      g_noalloc_ptr[dev] = (double *)p;
-    }
-    scratch = g_noalloc_ptr[dev];
+    std::lock_guard<std::mutex> lk(g_dev_mutex);
+    scratch = g_noalloc_ptr[dev];  // resolved by TDySetup on this device
   }
+  if (!scratch) return set_error(TDY_ERR_LIB, "static scratch address of device %d was not resolved at set-up", dev);
   cudaStream_t st = stream ? (cudaStream_t)stream : d->stream;
   DevArgs a = d->a;
   a.form = FORM_SNES;
@@ -1578,7 +1677,10 @@ int device_eval_noalloc(_p_TDy *t, const double *dU, double *dR, double *dJ, voi
   a.R = dR;
   a.J = dJ;
   a.scratch = scratch;
-  return launch_eval(a, st, nullptr);
+  int ierr = launch_eval(a, st, nullptr);
+  if (ierr) return ierr;
+  CUDA_TRY(cudaEventRecord(d->noalloc_ev, st));
+  return 0;
 }
 
 int device_launches_per_eval(_p_TDy *t) {

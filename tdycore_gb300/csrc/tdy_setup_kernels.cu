@@ -222,19 +222,22 @@ __global__ void __launch_bounds__(64) canon_trans_kernel(SetupGeom g, double *Tc
   }
 }
 
+// stream-ordered temporary (v must stay alive until the stream is synchronised)
 template <class T>
-int upload(std::vector<void *> &owned, T **p, const std::vector<T> &v) {
-  cudaError_t e = cudaMalloc((void **)p, v.size() * sizeof(T) + 1);
-  if (e != cudaSuccess) return set_error(TDY_ERR_GPU, "cudaMalloc: %s", cudaGetErrorString(e));
+int upload(std::vector<void *> &owned, T **p, const std::vector<T> &v, cudaStream_t st) {
+  int ierr = dmem_alloc((void **)p, v.size() * sizeof(T) + 1, st);
+  if (ierr) return ierr;
   owned.push_back(*p);
-  e = cudaMemcpy(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
-  if (e != cudaSuccess) return set_error(TDY_ERR_GPU, "cudaMemcpy: %s", cudaGetErrorString(e));
+  if (v.empty()) return 0;
+  cudaError_t e = cudaMemcpyAsync(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return set_error(TDY_ERR_GPU, "cudaMemcpyAsync: %s", cudaGetErrorString(e));
   return 0;
 }
 
 }  // namespace
 
-int device_canon_trans(const _p_TDy *t, const int *d_cellc, const int *d_facec, double *d_Tc) {
+int device_canon_trans(const _p_TDy *t, const int *d_cellc, const int *d_facec, double *d_Tc, void *stream) {
+  cudaStream_t cs = (cudaStream_t)stream;
   const Mesh &m = t->mesh;
   const MPFAOSetup &s = t->setup;
   if (s.nC == 0) return 0;
@@ -249,44 +252,46 @@ int device_canon_trans(const _p_TDy *t, const int *d_cellc, const int *d_facec, 
   std::vector<double> sub(m.nf);
   for (int f = 0; f < m.nf; f++) sub[f] = m.face_area[f] / (m.face_vert_off[f + 1] - m.face_vert_off[f]);
   int *st = nullptr;
+  const std::vector<int> zero(1, 0);
   {
     int *p;
     double *q;
-    if ((ierr = upload(owned, &p, s.canon_vertex))) goto done;
+    if ((ierr = upload(owned, &p, s.canon_vertex, cs))) goto done;
     g.canon_vertex = p;
-    if ((ierr = upload(owned, &p, m.face_cell0))) goto done;
+    if ((ierr = upload(owned, &p, m.face_cell0, cs))) goto done;
     g.face_cell0 = p;
-    if ((ierr = upload(owned, &p, m.face_cell1))) goto done;
+    if ((ierr = upload(owned, &p, m.face_cell1, cs))) goto done;
     g.face_cell1 = p;
-    if ((ierr = upload(owned, &q, m.vx))) goto done;
+    if ((ierr = upload(owned, &q, m.vx, cs))) goto done;
     g.vx = q;
-    if ((ierr = upload(owned, &q, m.cell_cen))) goto done;
+    if ((ierr = upload(owned, &q, m.cell_cen, cs))) goto done;
     g.cell_cen = q;
-    if ((ierr = upload(owned, &q, m.face_cen))) goto done;
+    if ((ierr = upload(owned, &q, m.face_cen, cs))) goto done;
     g.face_cen = q;
-    if ((ierr = upload(owned, &q, m.face_nrm))) goto done;
+    if ((ierr = upload(owned, &q, m.face_nrm, cs))) goto done;
     g.face_nrm = q;
-    if ((ierr = upload(owned, &q, sub))) goto done;
+    if ((ierr = upload(owned, &q, sub, cs))) goto done;
     g.subface_area = q;
-    if ((ierr = upload(owned, &q, t->mat.K0))) goto done;
+    if ((ierr = upload(owned, &q, t->mat.K0, cs))) goto done;
     g.K0 = q;
-    if ((ierr = upload(owned, &st, std::vector<int>(1, 0)))) goto done;
+    if ((ierr = upload(owned, &st, zero, cs))) goto done;
   }
   {
     const int bs = 64;
-    canon_trans_kernel<<<(s.nC + bs - 1) / bs, bs>>>(g, d_Tc, st);
+    canon_trans_kernel<<<(s.nC + bs - 1) / bs, bs, 0, cs>>>(g, d_Tc, st);
+    int hs = 0;
     cudaError_t e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&hs, st, sizeof(int), cudaMemcpyDeviceToHost, cs);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(cs);
     if (e != cudaSuccess) {
       ierr = set_error(TDY_ERR_GPU, "canon_trans_kernel: %s", cudaGetErrorString(e));
       goto done;
     }
-    int hs = 0;
-    cudaMemcpy(&hs, st, sizeof(int), cudaMemcpyDeviceToHost);
     if (hs) ierr = set_error(TDY_ERR_LIB, "singular interaction-region system at an interior hexahedral vertex");
   }
 done:
-  for (void *p : owned) cudaFree(p);
+  cudaStreamSynchronize(cs);  // the uploads have read their host vectors
+  for (void *p : owned) dmem_free(p, cs);
   return ierr;
 }
 

@@ -13,7 +13,9 @@
 //     coupling of each column of an extruded block, Thomas algorithm, one
 //     thread per column), which carries the stiff vertical coupling of thin
 //     layers;
-//   * one BiCGStab iteration is captured once as a CUDA graph and replayed;
+//   * one BiCGStab iteration is built once as a CUDA graph with the explicit
+//     graph API (kernel nodes in a chain, no stream capture, so device calls
+//     that other threads make meanwhile cannot invalidate it) and replayed;
 //   * the sparse matrix-vector product's threads per row (1, 4 or 8) are
 //     picked by timing the candidates on the first solve.
 // No reference counterpart: the reference hands F and J to PETSc's SNES/KSP.
@@ -23,6 +25,8 @@
 #include <cmath>
 #include <cstring>
 #include <mutex>
+#include <tuple>
+#include <utility>
 #include <vector>
 
 #include "tdy_device.h"
@@ -40,6 +44,47 @@ namespace {
 
 inline unsigned nblk(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
+// Kernel launches of the solver go through an Emit: straight to its stream,
+// or, while a graph is being built, as the next kernel node of a chain in
+// that graph (the explicit graph API: the kernel's arguments are converted
+// to its parameter types and copied into the node).  Empty grids launch
+// nothing in either mode.
+struct Emit {
+  cudaStream_t st = nullptr;
+  cudaGraph_t g = nullptr;
+  cudaGraphNode_t last = nullptr;
+  cudaError_t err = cudaSuccess;
+  explicit Emit(cudaStream_t s) : st(s) {}
+  template <class... P, class... A>
+  void operator()(void (*k)(P...), unsigned grid, unsigned block, size_t smem, A... args) {
+    static_assert(sizeof...(P) == sizeof...(A), "kernel argument count");
+    if (grid == 0) return;
+    if (!g) {
+      k<<<grid, block, smem, st>>>(args...);
+      return;
+    }
+    if (err != cudaSuccess) return;
+    std::tuple<P...> vals(args...);
+    add_node((void *)k, grid, block, smem, vals, std::index_sequence_for<P...>{});
+  }
+
+ private:
+  template <class Tup, size_t... I>
+  void add_node(void *fn, unsigned grid, unsigned block, size_t smem, Tup &vals, std::index_sequence<I...>) {
+    void *ptrs[sizeof...(I) > 0 ? sizeof...(I) : 1] = {(void *)&std::get<I>(vals)...};
+    cudaKernelNodeParams p = {};
+    p.func = fn;
+    p.gridDim = dim3(grid);
+    p.blockDim = dim3(block);
+    p.sharedMemBytes = (unsigned)smem;
+    p.kernelParams = ptrs;
+    p.extra = nullptr;
+    cudaGraphNode_t n = nullptr;
+    err = cudaGraphAddKernelNode(&n, g, last ? &last : nullptr, last ? 1 : 0, &p);
+    if (err == cudaSuccess) last = n;
+  }
+};
+
 // per-instance scalars, [slot][nseg]
 enum { S_RHO = 0, S_ALPHA, S_OMEGA, S_BETA, S_BNORM2, S_T1, S_T2, S_HALF, S_NSCAL };
 
@@ -53,8 +98,7 @@ struct Krylov {
   void *clu = nullptr;                                 // clusters: LU factors (T), grown on demand
   size_t clu_cap = 0;                                  // elements of clu
   cudaGraphExec_t graph = nullptr;
-  cudaStream_t graph_stream = nullptr;
-  int graph_precond = -1;  // preconditioner the graph was captured with
+  int graph_precond = -1;  // preconditioner the graph was built with
   int tpr = 0;  // spmv threads per row (autotuned)
 };
 
@@ -80,17 +124,22 @@ struct SolverState {
   int *clab = nullptr, *cflag = nullptr, *cloc = nullptr, *cmem = nullptr, *coff = nullptr, *cpiv = nullptr;
   long long *cluoff = nullptr;
   int ncl = 0;  // clusters of 2..64 cells in the current solve
+  int ncl_cells = 0, ncl_big_cells = 0;  // cells in them; cells of clusters over 64 cells
   int precond_used = 0;
   std::vector<int> h_lab, h_cnt, h_id, h_fill, h_loc, h_mem, h_off;
   std::vector<long long> h_luoff;
   Krylov k32, k64;
+  // device memory: stream-ordered on the handle's stream (allocated there and
+  // synchronised at init; freed there when the solver is destroyed, after
+  // every solve has synchronised its stream)
+  cudaStream_t st = nullptr;
   std::vector<void *> allocs;
   ~SolverState() {
     for (Krylov *k : {&k32, &k64}) {
       if (k->graph) cudaGraphExecDestroy(k->graph);
-      if (k->clu) cudaFree(k->clu);
+      if (k->clu) dmem_free(k->clu, st);
     }
-    for (void *p : allocs) cudaFree(p);
+    for (void *p : allocs) dmem_free(p, st);
   }
 };
 
@@ -98,17 +147,19 @@ namespace {
 
 template <class T>
 int salloc(SolverState *s, T **p, size_t n) {
-  cudaError_t e = cudaMalloc((void **)p, std::max<size_t>(n, 1) * sizeof(T));
-  if (e != cudaSuccess) return set_error(TDY_ERR_GPU, "cudaMalloc: %s", cudaGetErrorString(e));
+  int ierr = dmem_alloc((void **)p, std::max<size_t>(n, 1) * sizeof(T), s->st);
+  if (ierr) return ierr;
   s->allocs.push_back(*p);
   return 0;
 }
+// (the host vector must stay alive until the stream is synchronised)
 template <class T>
 int sup(SolverState *s, T **p, const std::vector<T> &h) {
   int ierr = salloc(s, p, h.size());
   if (ierr) return ierr;
-  cudaError_t e = cudaMemcpy(*p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice);
-  if (e != cudaSuccess) return set_error(TDY_ERR_GPU, "cudaMemcpy: %s", cudaGetErrorString(e));
+  if (h.empty()) return 0;
+  cudaError_t e = cudaMemcpyAsync(*p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s->st);
+  if (e != cudaSuccess) return set_error(TDY_ERR_GPU, "cudaMemcpyAsync: %s", cudaGetErrorString(e));
   return 0;
 }
 
@@ -512,76 +563,86 @@ __global__ void __launch_bounds__(32) cl_apply_kernel(int ncl, const int *coff, 
 
 // ---------------------------------------------------------------------------
 template <class T>
-int spmv(SolverState *s, const Krylov &k, const T *x, T *y, cudaStream_t st) {
+int spmv(SolverState *s, const Krylov &k, const T *x, T *y, Emit &e) {
   const T *A = (const T *)k.Jv;
-  const long long threads = (long long)s->n * k.tpr;
+  const unsigned g = nblk((long long)s->n * k.tpr, 256);
   switch (k.tpr) {
     case 1:
-      spmv_kernel<T, 1><<<nblk(threads, 256), 256, 0, st>>>(s->n, s->rowptr, s->colidx, A, x, y);
+      e(spmv_kernel<T, 1>, g, 256, 0, s->n, (const int *)s->rowptr, (const int *)s->colidx, A, x, y);
       break;
     case 4:
-      spmv_kernel<T, 4><<<nblk(threads, 256), 256, 0, st>>>(s->n, s->rowptr, s->colidx, A, x, y);
+      e(spmv_kernel<T, 4>, g, 256, 0, s->n, (const int *)s->rowptr, (const int *)s->colidx, A, x, y);
       break;
     default:
-      spmv_kernel<T, 8><<<nblk(threads, 256), 256, 0, st>>>(s->n, s->rowptr, s->colidx, A, x, y);
+      e(spmv_kernel<T, 8>, g, 256, 0, s->n, (const int *)s->rowptr, (const int *)s->colidx, A, x, y);
       break;
   }
   return 0;
 }
 
 template <class TA, class TB>
+void seg_dot(SolverState *s, const TA *a, const TB *b, const TA *c, const TB *d, double *out, double *out2, Emit &e) {
+  e(chunk_dot_kernel<TA, TB>, (unsigned)s->nchunks, 256, 0, (const int *)s->chunk_off, a, b, c, d, s->part,
+    s->part2);
+  e(chunk_sum_kernel, nblk(s->nseg, 128), 128, 0, s->nseg, (const int *)s->seg_chunk, (const double *)s->part,
+    (const double *)s->part2, out, c ? out2 : (double *)nullptr);
+}
+template <class TA, class TB>
 void seg_dot(SolverState *s, const TA *a, const TB *b, const TA *c, const TB *d, double *out, double *out2,
              cudaStream_t st) {
-  chunk_dot_kernel<TA, TB><<<s->nchunks, 256, 0, st>>>(s->chunk_off, a, b, c, d, s->part, s->part2);
-  chunk_sum_kernel<<<nblk(s->nseg, 128), 128, 0, st>>>(s->nseg, s->seg_chunk, s->part, s->part2, out,
-                                                       c ? out2 : nullptr);
+  Emit e(st);
+  seg_dot<TA, TB>(s, a, b, c, d, out, out2, e);
 }
 
 template <class T>
-int dot(SolverState *s, const T *a, const T *b, const T *c, const T *d, int slot1, int slot2, cudaStream_t st) {
-  seg_dot<T, T>(s, a, b, c, d, s->scal + (size_t)slot1 * s->nseg, c ? s->scal + (size_t)slot2 * s->nseg : nullptr, st);
+int dot(SolverState *s, const T *a, const T *b, const T *c, const T *d, int slot1, int slot2, Emit &e) {
+  seg_dot<T, T>(s, a, b, c, d, s->scal + (size_t)slot1 * s->nseg, c ? s->scal + (size_t)slot2 * s->nseg : nullptr, e);
   return 0;
 }
 
 // out = M^-1 in with the preconditioner of the current solve
 template <class T>
-void precondition(SolverState *s, Krylov &k, const T *in, T *out, cudaStream_t st) {
+void precondition(SolverState *s, Krylov &k, const T *in, T *out, Emit &e) {
   if (s->precond_used == TDY_PRECOND_CLUSTERS) {
-    cl_apply_diag_kernel<T><<<nblk(s->n, 256), 256, 0, st>>>(s->n, s->cloc, (const T *)k.cinv, in, out);
-    if (s->ncl > 0)
-      cl_apply_kernel<T><<<s->ncl, 32, 0, st>>>(s->ncl, s->coff, s->cluoff, s->cmem, (const T *)k.clu, s->cpiv, in,
-                                                out);
+    e(cl_apply_diag_kernel<T>, nblk(s->n, 256), 256, 0, s->n, (const int *)s->cloc, (const T *)k.cinv, in, out);
+    e(cl_apply_kernel<T>, (unsigned)s->ncl, 32, 0, s->ncl, (const int *)s->coff, (const long long *)s->cluoff,
+      (const int *)s->cmem, (const T *)k.clu, (const int *)s->cpiv, in, out);
   } else {
-    line_solve_kernel<T><<<nblk(s->nlines, 128), 128, 0, st>>>(s->nlines, s->line_off, s->line_cells,
-                                                                (const T *)k.la, (const T *)k.lcp, (const T *)k.linv,
-                                                                in, out);
+    e(line_solve_kernel<T>, nblk(s->nlines, 128), 128, 0, s->nlines, (const int *)s->line_off,
+      (const int *)s->line_cells, (const T *)k.la, (const T *)k.lcp, (const T *)k.linv, in, out);
   }
 }
 
 // one BiCGStab iteration for every active instance (the graph body)
 template <class T>
-void bicgstab_iteration(SolverState *s, Krylov &k, double tol2, cudaStream_t st) {
+void bicgstab_iteration(SolverState *s, Krylov &k, double tol2, Emit &e) {
   const int n = s->n, ns = s->nseg;
   const unsigned gb = nblk(n, 256), sb = nblk(ns, 128);
   T *r = (T *)k.r, *r0 = (T *)k.r0, *p = (T *)k.p, *v = (T *)k.v, *sv = (T *)k.s, *tv = (T *)k.t;
   T *ph = (T *)k.ph, *sh = (T *)k.sh, *y = (T *)k.y;
-  dot<T>(s, r0, r, nullptr, nullptr, S_T1, 0, st);
-  scal_beta_kernel<<<sb, 128, 0, st>>>(ns, s->lin_active, s->scal);
-  p_update_kernel<T><<<gb, 256, 0, st>>>(n, s->cell_seg, s->lin_active, s->scal, ns, r, v, p);
-  precondition<T>(s, k, p, ph, st);
-  spmv<T>(s, k, ph, v, st);
-  dot<T>(s, r0, v, nullptr, nullptr, S_T1, 0, st);
-  scal_alpha_kernel<<<sb, 128, 0, st>>>(ns, s->lin_active, s->scal);
-  s_update_kernel<T><<<gb, 256, 0, st>>>(n, s->cell_seg, s->lin_active, s->scal, ns, r, v, sv);
-  dot<T>(s, sv, sv, nullptr, nullptr, S_T1, 0, st);
-  scal_half_kernel<<<sb, 128, 0, st>>>(ns, s->lin_active, s->scal, tol2);
-  precondition<T>(s, k, sv, sh, st);
-  spmv<T>(s, k, sh, tv, st);
-  dot<T>(s, tv, tv, tv, sv, S_T1, S_T2, st);
-  scal_omega_kernel<<<sb, 128, 0, st>>>(ns, s->lin_active, s->scal);
-  xr_update_kernel<T><<<gb, 256, 0, st>>>(n, s->cell_seg, s->lin_active, s->scal, ns, ph, sh, sv, tv, y, r);
-  dot<T>(s, r, r, nullptr, nullptr, S_T1, 0, st);
-  scal_check_kernel<<<sb, 128, 0, st>>>(ns, s->lin_active, s->lin_its, s->scal, tol2);
+  const int *cs = s->cell_seg;
+  int *act = s->lin_active;
+  const int *cact = s->lin_active;
+  double *sc = s->scal;
+  const double *csc = s->scal;
+  dot<T>(s, r0, r, nullptr, nullptr, S_T1, 0, e);
+  e(scal_beta_kernel, sb, 128, 0, ns, act, sc);
+  e(p_update_kernel<T>, gb, 256, 0, n, cs, cact, csc, ns, (const T *)r, (const T *)v, p);
+  precondition<T>(s, k, p, ph, e);
+  spmv<T>(s, k, ph, v, e);
+  dot<T>(s, r0, v, nullptr, nullptr, S_T1, 0, e);
+  e(scal_alpha_kernel, sb, 128, 0, ns, act, sc);
+  e(s_update_kernel<T>, gb, 256, 0, n, cs, cact, csc, ns, (const T *)r, (const T *)v, sv);
+  dot<T>(s, sv, sv, nullptr, nullptr, S_T1, 0, e);
+  e(scal_half_kernel, sb, 128, 0, ns, cact, sc, tol2);
+  precondition<T>(s, k, sv, sh, e);
+  spmv<T>(s, k, sh, tv, e);
+  dot<T>(s, tv, tv, tv, sv, S_T1, S_T2, e);
+  e(scal_omega_kernel, sb, 128, 0, ns, cact, sc);
+  e(xr_update_kernel<T>, gb, 256, 0, n, cs, cact, csc, ns, (const T *)ph, (const T *)sh, (const T *)sv,
+    (const T *)tv, y, r);
+  dot<T>(s, r, r, nullptr, nullptr, S_T1, 0, e);
+  e(scal_check_kernel, sb, 128, 0, ns, act, s->lin_its, sc, tol2);
 }
 
 template <class T>
@@ -621,11 +682,12 @@ int autotune_spmv(SolverState *s, Krylov &k, cudaStream_t st) {
   SCUDA(cudaEventCreate(&e1));
   float best = 1e30f;
   int best_tpr = 1;
+  Emit em(st);
   for (int tpr : {1, 4, 8}) {
     k.tpr = tpr;
-    spmv<T>(s, k, (const T *)k.b, (T *)k.v, st);  // warm-up
+    spmv<T>(s, k, (const T *)k.b, (T *)k.v, em);  // warm-up
     cudaEventRecord(e0, st);
-    for (int it = 0; it < 5; it++) spmv<T>(s, k, (const T *)k.b, (T *)k.v, st);
+    for (int it = 0; it < 5; it++) spmv<T>(s, k, (const T *)k.b, (T *)k.v, em);
     cudaEventRecord(e1, st);
     SCUDA(cudaEventSynchronize(e1));
     float ms = 0.f;
@@ -698,13 +760,17 @@ int cluster_setup(SolverState *s, Krylov &k, double tau, cudaStream_t st) {
   id.assign(n, -1);
   off.assign(1, 0);
   luoff.assign(1, 0);
-  int ncl = 0;
+  int ncl = 0, big = 0;
   for (int r = 0; r < n; r++)
     if (cnt[r] >= 2 && cnt[r] <= kClusterMax) {
       id[r] = ncl++;
       off.push_back(off.back() + cnt[r]);
       luoff.push_back(luoff.back() + (long long)cnt[r] * cnt[r]);
+    } else if (cnt[r] > kClusterMax) {
+      big += cnt[r];
     }
+  s->ncl_cells = off.back();
+  s->ncl_big_cells = big;
   fill.assign(ncl, 0);
   loc.assign(n, -1);
   mem.resize(off.back());
@@ -721,12 +787,11 @@ int cluster_setup(SolverState *s, Krylov &k, double tau, cudaStream_t st) {
     SCUDA(cudaMemcpyAsync(s->coff, off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice, st));
     SCUDA(cudaMemcpyAsync(s->cluoff, luoff.data(), sizeof(long long) * luoff.size(), cudaMemcpyHostToDevice, st));
     const size_t need = (size_t)luoff.back();
-    if (need > k.clu_cap) {
-      SCUDA(cudaStreamSynchronize(st));
-      if (k.clu) cudaFree(k.clu);
+    if (need > k.clu_cap) {  // stream-ordered: no device synchronisation
+      if (k.clu) dmem_free(k.clu, st);
       k.clu = nullptr;
       k.clu_cap = 0;
-      SCUDA(cudaMalloc(&k.clu, need * sizeof(T)));
+      if ((ierr = dmem_alloc(&k.clu, need * sizeof(T), st))) return ierr;
       k.clu_cap = need;
     }
   }
@@ -756,24 +821,35 @@ int linear_solve(SolverState *s, Krylov &k, const TDyNewtonOptions &o, cudaStrea
                                                                  s->pos_hi, s->J, (T *)k.la, (T *)k.lcp, (T *)k.linv);
   init_kernel<T><<<nblk(n, 256), 256, 0, st>>>(n, s->cell_seg, s->newt_active, s->F, (T *)k.b, (T *)k.r, (T *)k.r0,
                                                (T *)k.p, (T *)k.v, (T *)k.y);
-  dot<T>(s, (T *)k.b, (T *)k.b, nullptr, nullptr, S_BNORM2, 0, st);
+  {
+    Emit em(st);
+    dot<T>(s, (T *)k.b, (T *)k.b, nullptr, nullptr, S_BNORM2, 0, em);
+  }
   SCUDA(cudaMemsetAsync(s->lin_its, 0, sizeof(int) * ns, st));
   init_scalars_kernel<<<nblk(ns, 128), 128, 0, st>>>(ns, s->newt_active, s->lin_active, s->lin_its, s->scal);
   SCUDA(cudaGetLastError());
   const double tol2 = o.linear_rtol * o.linear_rtol;
-  // the cluster launches depend on this solve's cluster count: recapture
-  if (!k.graph || k.graph_stream != st || s->linear_rtol != o.linear_rtol || k.graph_precond != s->precond_used ||
+  // The graph of one iteration is built with the explicit graph API, not by
+  // stream capture: a capture is invalidated by device-wide operations that
+  // other threads issue meanwhile (a cudaFree, a device synchronisation),
+  // which a server running many handles at once cannot rule out.  The cluster
+  // launches depend on this solve's cluster count: rebuild for every solve.
+  if (!k.graph || s->linear_rtol != o.linear_rtol || k.graph_precond != s->precond_used ||
       s->precond_used == TDY_PRECOND_CLUSTERS) {
     if (k.graph) cudaGraphExecDestroy(k.graph);
     k.graph = nullptr;
-    cudaGraph_t g;
-    SCUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    bicgstab_iteration<T>(s, k, tol2, st);
-    SCUDA(cudaStreamEndCapture(st, &g));
-    cudaError_t e = cudaGraphInstantiate(&k.graph, g, 0);
+    cudaGraph_t g = nullptr;
+    SCUDA(cudaGraphCreate(&g, 0));
+    Emit em(st);
+    em.g = g;
+    bicgstab_iteration<T>(s, k, tol2, em);
+    cudaError_t e = em.err;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&k.graph, g, 0);
     cudaGraphDestroy(g);
-    if (e != cudaSuccess) return set_error(TDY_ERR_GPU, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
-    k.graph_stream = st;
+    if (e != cudaSuccess) {
+      k.graph = nullptr;
+      return set_error(TDY_ERR_GPU, "BiCGStab iteration graph: %s", cudaGetErrorString(e));
+    }
     k.graph_precond = s->precond_used;
     s->linear_rtol = o.linear_rtol;
   }
@@ -799,6 +875,7 @@ int solver_init(_p_TDy *t) {
   const MPFAOSetup &su = t->setup;
   SolverState *s = new SolverState();
   t->solver = s;
+  s->st = (cudaStream_t)device_default_stream(t);
   s->n = t->mesh.nc;
   s->nnz = (int)su.colidx.size();
   // instances: the mesh blocks; lines: the columns of each block, bottom to top
@@ -849,11 +926,9 @@ int solver_init(_p_TDy *t) {
   if ((ierr = sup(s, &s->line_off, line_off))) return ierr;
   if ((ierr = sup(s, &s->line_cells, line_cells))) return ierr;
   if ((ierr = sup(s, &s->pos_d, pd))) return ierr;
-  {
-    std::vector<int> dp(s->n);
-    for (int i = 0; i < s->n; i++) dp[i] = find(i, i);  // every row has its diagonal (checked above per line cell)
-    if ((ierr = sup(s, &s->dpos, dp))) return ierr;
-  }
+  std::vector<int> dp(s->n);
+  for (int i = 0; i < s->n; i++) dp[i] = find(i, i);  // every row has its diagonal (checked above per line cell)
+  if ((ierr = sup(s, &s->dpos, dp))) return ierr;
   if ((ierr = sup(s, &s->pos_lo, plo))) return ierr;
   if ((ierr = sup(s, &s->pos_hi, phi))) return ierr;
   if ((ierr = salloc(s, &s->x, s->n))) return ierr;
@@ -868,6 +943,9 @@ int solver_init(_p_TDy *t) {
   if ((ierr = salloc(s, &s->newt_active, s->nseg))) return ierr;
   if ((ierr = salloc(s, &s->lin_active, s->nseg))) return ierr;
   if ((ierr = salloc(s, &s->lin_its, s->nseg))) return ierr;
+  // the allocations and uploads complete before any other stream uses them
+  // (and before the host vectors above go out of scope)
+  SCUDA(cudaStreamSynchronize(s->st));
   return 0;
 }
 
@@ -1041,12 +1119,14 @@ int device_be_solve(_p_TDy *t, double dt, double *dU, const TDyNewtonOptions &o,
   }
   SCUDA(cudaMemcpyAsync(dU, s->xb, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
   SCUDA(cudaStreamSynchronize(st));
-  int conv = 0, maxit = 0;
+  int conv = 0, conv_step = 0, maxit = 0;
   double worst = 0.0;
   for (int g = 0; g < ns; g++) {
     const double rel = f0[g] > 0.0 ? fn[g] / f0[g] : 0.0;
-    const bool ok = !failed[g] && std::isfinite(fn[g]) && (!(fn[g] > o.atol) || rel <= o.rtol || step_conv[g]);
+    const bool fin = !failed[g] && std::isfinite(fn[g]);
+    const bool ok = fin && (!(fn[g] > o.atol) || rel <= o.rtol);
     conv += ok ? 1 : 0;
+    conv_step += (fin && !ok && step_conv[g]) ? 1 : 0;
     worst = std::max(worst, rel);
     maxit = std::max(maxit, its[g]);
     if (inst_its) inst_its[g] = its[g];
@@ -1058,6 +1138,11 @@ int device_be_solve(_p_TDy *t, double dt, double *dU, const TDyNewtonOptions &o,
     stats->converged = conv;
     stats->ninstances = ns;
     stats->max_rel_residual = worst;
+    stats->step_converged = conv_step;
+    stats->precond_used = s->precond_used;
+    stats->clusters = s->precond_used == TDY_PRECOND_CLUSTERS ? s->ncl : 0;
+    stats->cluster_cells = s->precond_used == TDY_PRECOND_CLUSTERS ? s->ncl_cells : 0;
+    stats->cluster_cells_diagonal = s->precond_used == TDY_PRECOND_CLUSTERS ? s->ncl_big_cells : 0;
   }
   return 0;
 }

@@ -54,6 +54,7 @@ class Request:
     newton_its: list = field(default_factory=list)
     rel_residual: list = field(default_factory=list)
     converged_steps: int = 0
+    step_test_steps: int = 0  # steps ended by the step test above the tolerance
     error: str | None = None
 
     @property
@@ -130,6 +131,12 @@ def run_request(req: Request, fp32: bool = True, dt: float = 3600.0, rtol: float
             stats, its, rel = t.backward_euler_step_device(dU, dt, rtol=rtol, fp32=fp32)
             req.newton_its.append(int(its[0]))
             req.rel_residual.append(float(rel[0]))
+            if stats["step_converged"] == 1:
+                # Newton stopped on a negligible step above the tolerance (as
+                # PETSc's step test does): the request goes on, but the step
+                # is not counted as a solve at the tolerance
+                req.step_test_steps += 1
+                continue
             if stats["converged"] != 1:
                 # the request ends here: later steps from an unconverged state
                 # would mean nothing to the caller
@@ -227,6 +234,7 @@ def summary(reqs, wall_s: float):
     attempted = sum(len(r.rel_residual) for r in reqs)
     errs = [f"{r.rid}: {r.error}" for r in reqs if r.error is not None]
     return {"requests": len(reqs), "errors": len(errs), "error_messages": errs[:3],
+            "step_test_steps": sum(r.step_test_steps for r in reqs),
             "p50_latency_s": float(np.percentile(lat, 50)) if lat.size else None,
             "p99_latency_s": float(np.percentile(lat, 99)) if lat.size else None,
             "solves_per_s": steps / wall_s, "converged_solves": steps, "solves_attempted": attempted,

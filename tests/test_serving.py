@@ -84,9 +84,29 @@ def test_same_result_alone_and_in_the_mix():
     srv = S.Server(slots=4)
     mix = srv.run(reqs)
     assert all(r.error is None for r in mix), [r.error for r in mix]
-    assert all(r.converged_steps == 3 for r in mix)
+    assert all(r.converged_steps + r.step_test_steps == 3 for r in mix)
     for k in (0, 5):
         alone = S.make_requests(8, rate_per_s=400.0, nsteps=3, large_fraction=0.0, seed=5)[k]
         S.run_request(alone)
         assert np.array_equal(alone.U_final, mix[k].U_final)
         assert alone.newton_its == mix[k].newton_its
+
+
+@pytest.mark.gpu
+def test_concurrent_requests_with_overlapping_setup_and_teardown():
+    """24 requests arriving at once on 16 slots: while some requests iterate
+    (and build their inner-solve graphs), others set up or destroy their
+    handles.  No request may fail for any reason but a step that does not
+    converge, and a request's result is the same as when it runs alone."""
+    reqs = S.make_requests(24, rate_per_s=5000.0, nsteps=2, large_fraction=0.0, seed=11)
+    srv = S.Server(slots=16)
+    done = srv.run(reqs)
+    assert srv.peak_running >= 16
+    bad = [r.error for r in done if r.error is not None and "did not converge" not in r.error]
+    assert not bad, bad
+    assert sum(r.converged_steps + r.step_test_steps for r in done) >= 40
+    for k in (3, 17):
+        alone = S.make_requests(24, rate_per_s=5000.0, nsteps=2, large_fraction=0.0, seed=11)[k]
+        S.run_request(alone)
+        assert alone.error == done[k].error
+        assert np.array_equal(alone.U_final, done[k].U_final)
