@@ -141,13 +141,38 @@ def algorithmic_bytes(view):
 
 
 def vertex_kernel_bytes(view):
-    """Algorithmic bytes of one vertex_kernel launch: its Trans blocks, one
-    gravity coefficient per row, one read of the per-cell/per-boundary state it
-    upwinds on (P, rho, drho, lam, dlam) and its per-vertex partial outputs."""
-    nint = view["v_nint"].astype(np.int64)
-    partials = int(np.sum(nint * nint + nint))
-    nb = view["nbnd"]
-    return 8 * (int(view["ntrans_total"]) + int(view["nrows_total"]) + 5 * (view["ncells"] + nb) + partials)
+    """The vertex stage's share of the algorithmic bytes (the formula of
+    algorithmic_bytes): its Trans blocks, one gravity coefficient per row and
+    the cell pressures, 8 * (sum_v R_v C_v + sum_v R_v + Nc).  The state it
+    gathers beyond P and the per-vertex partial sums it hands to the cell
+    stage are intermediate data of this implementation, not algorithmic
+    bytes."""
+    return 8 * (int(view["ntrans_total"]) + int(view["nrows_total"]) + int(view["ncells"]))
+
+
+def workload_config(info, nc, nnz, world):
+    """The workload description, identical in both arms of the bench."""
+    return {"workload": info["workload"], "ncells": nc, "nnz_jacobian": nnz, "form": "SNES F+J",
+            "seed": info["seed"], "l2": "inputs larger than L2 (no flush)",
+            "parallelism": f"replicas x{world}" if world > 1 else "one device"}
+
+
+def fp64_pipe_from_profile(kernel_ms):
+    """FP64 pipe utilisation per kernel from the committed ncu summary
+    (sm__pipe_fp64_cycles_active), and its average over one evaluation
+    weighted by the live per-kernel durations."""
+    f = ROOT / "profiles" / "fp64_pipe.json"
+    if not f.exists():
+        return None
+    try:
+        d = json.loads(f.read_text())
+    except Exception:
+        return None
+    per = d.get("pipe_fp64_active_frac", {})
+    tot = sum(kernel_ms.get(k, 0.0) for k in per)
+    avg = sum(per[k] * kernel_ms.get(k, 0.0) for k in per) / tot if tot > 0 else None
+    return {"per_kernel": per, "evaluation_time_weighted": avg, "source": "profiles/fp64_pipe.json",
+            "captured_workload": d.get("captured_workload")}
 
 
 def fp64_flops_per_eval(view):
@@ -177,12 +202,15 @@ def make_oracle(view, Uprev):
 def parity_full_size(o, U, R, J):
     """Largest error of the GPU R and J against the oracle at the bench
     workload, in units of the oracle's per-entry error scale (the parity tests
-    require <= 1e-12 for R and <= 1e-10 for J)."""
+    require <= 1e-12 for R and <= 1e-10 for J), and the norm-wise residual
+    error ||R - R_ref||_2 / ||R_ref||_2 (the state is perturbed, far from
+    equilibrium)."""
     Rr, Rm = o.snes_function(U, with_mag=True)
     Jr, Jm = o.snes_jacobian(U, with_mag=True)
     tiny = np.finfo(float).tiny
     return (float(np.max(np.abs(R - Rr) / np.maximum(Rm, tiny))),
-            float(np.max(np.abs(J - Jr) / np.maximum(Jm, tiny))))
+            float(np.max(np.abs(J - Jr) / np.maximum(Jm, tiny))),
+            float(np.linalg.norm(R - Rr) / np.linalg.norm(Rr)))
 
 
 def newton_config1():
@@ -227,10 +255,12 @@ def newton_config1():
 def batched_config4(ninst=4096, sample=64, dt=3600.0):
     """Config 4: independent hexahedral subdomains (nx, ny ~ U{1..8}, nz ~
     U{10..100}) in one handle, each advanced one backward-Euler step of
-    3600 s to a relative FP64 residual of 1e-8 by the device Newton with
-    FP32 Jacobian and inner solve, against the same instances solved one by
-    one on the plain FP64 path (FP64 Jacobian and inner solve), timed on a
-    sample of them.  Every instance's result is checked against the FP64 oracle."""
+    3600 s to a relative FP64 residual of 1e-8 by the device Newton, batched
+    with the FP32 Jacobian and inner solve and batched in plain FP64 (which
+    separates the gain of precision from the gain of batching), against the
+    same instances solved one by one on the plain FP64 path, timed on a
+    sample of them.  Every batched instance is checked against the FP64
+    oracle."""
     import torch
 
     import tdycore_gb300 as T
@@ -246,27 +276,42 @@ def batched_config4(ninst=4096, sample=64, dt=3600.0):
     log(f"config 4: {ninst} instances, {tb.ncells} cells, setup {setup_s:.1f} s")
     dev = torch.device("cuda")
     off = np.concatenate([[0], np.cumsum(info["instance_cells"])])
-    # warm-up (graph capture, spmv autotune), then the timed batched solve
-    d = torch.tensor(U0, dtype=torch.float64, device=dev)
-    tb.backward_euler_step_device(d, dt)
-    d.copy_(torch.tensor(U0, dtype=torch.float64, device=dev))
-    torch.cuda.synchronize()
-    t1 = time.perf_counter()
-    stats, its, rel = tb.backward_euler_step_device(d, dt)
-    torch.cuda.synchronize()
-    batch_s = time.perf_counter() - t1
-    Ub = d.cpu().numpy()
-    # FP64 oracle residual of every instance
+    seg = np.repeat(np.arange(ninst), info["instance_cells"])
     o = Oracle(tb.setup_view())
     o.snes_presolve(U0, dt)
-    F0 = o.snes_function(U0)
-    F1, M1 = o.snes_function(Ub, with_mag=True)
-    seg = np.repeat(np.arange(ninst), info["instance_cells"])
-    n0 = np.sqrt(np.bincount(seg, weights=F0 * F0, minlength=ninst))
-    n1 = np.sqrt(np.bincount(seg, weights=F1 * F1, minlength=ninst))
-    m1 = np.sqrt(np.bincount(seg, weights=M1 * M1, minlength=ninst))
-    rel_oracle = n1 / np.maximum(n0, 1e-300)
-    at_floor = n1 <= 1e-11 * m1
+    n0 = np.sqrt(np.bincount(seg, weights=o.snes_function(U0) ** 2, minlength=ninst))
+
+    def batched(fp32):
+        # warm-up (inner-solve graph, spmv autotune), then the timed batched solve
+        d = torch.tensor(U0, dtype=torch.float64, device=dev)
+        tb.backward_euler_step_device(d, dt, fp32=fp32)
+        d.copy_(torch.tensor(U0, dtype=torch.float64, device=dev))
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        stats, its, rel = tb.backward_euler_step_device(d, dt, fp32=fp32)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t1
+        Ub = d.cpu().numpy()
+        # FP64 oracle residual of every instance
+        F1, M1 = o.snes_function(Ub, with_mag=True)
+        n1 = np.sqrt(np.bincount(seg, weights=F1 * F1, minlength=ninst))
+        m1 = np.sqrt(np.bincount(seg, weights=M1 * M1, minlength=ninst))
+        rel_o = n1 / np.maximum(n0, 1e-300)
+        at_floor = n1 <= 1e-11 * m1
+        meets = (rel_o <= 1.01e-8) | at_floor
+        res = {"solves_per_s": ninst / wall, "batch_wall_s": wall,
+               "newton_iterations_max": stats["newton_iterations"],
+               "newton_iterations_mean": float(np.mean(its)), "linear_iterations_total": stats["linear_iterations"],
+               "converged": stats["converged"], "ended_by_step_test_above_rtol": stats["step_converged"],
+               "max_rel_residual_device": stats["max_rel_residual"],
+               "oracle_fp64": {"max_rel_residual": float(rel_o.max()),
+                               "instances_meeting_1e-8": int(np.sum(meets)),
+                               "instances_at_fp64_noise_floor": int(np.sum(at_floor & (rel_o > 1.01e-8)))}}
+        return res, Ub
+
+    fp32_res, Ub = batched(True)
+    fp64_res, Ub64 = batched(False)
+    fp64_res["max_rel_diff_vs_fp32_batch"] = float(np.max(np.abs(Ub64 - Ub) / np.abs(Ub64)))
     del o
     blocks, props = tb._blocks, tb._props
     tb.destroy()
@@ -305,40 +350,38 @@ def batched_config4(ninst=4096, sample=64, dt=3600.0):
     T.options_clear()
     one_by_one = len(pick) / solve_s
     return {
-        "workload": info["workload"], "ninstances": ninst, "ncells": int(off[-1]), "dt_s": dt,
-        "solves_per_s": ninst / batch_s, "batch_wall_s": batch_s, "setup_s": setup_s,
-        "newton_iterations_max": stats["newton_iterations"],
-        "newton_iterations_mean": float(np.mean(its)), "linear_iterations_total": stats["linear_iterations"],
-        "converged": stats["converged"], "max_rel_residual_device": stats["max_rel_residual"],
-        "oracle_fp64": {"max_rel_residual": float(rel_oracle.max()),
-                        "instances_meeting_1e-8": int(np.sum((rel_oracle <= 1.01e-8) | at_floor)),
-                        "note": "||F(U_new)|| / ||F(U_n)|| per instance from the FP64 oracle; an instance that "
-                                "starts within FP64 resolution of equilibrium counts when ||F|| is within 1e-11 "
-                                "of its error scale"},
+        "workload": info["workload"], "ninstances": ninst, "ncells": int(off[-1]), "dt_s": dt, "setup_s": setup_s,
+        "batched_fp32": fp32_res,
+        "batched_fp64": fp64_res,
         "one_by_one_fp64": {"solves_per_s": one_by_one, "sample": int(len(pick)),
-                            "max_rel_diff_vs_batched": max_diff,
+                            "max_rel_diff_vs_batched_fp32": max_diff,
                             "note": "the same instances, one handle each, FP64 Jacobian and inner solve; "
                                     "solve calls timed, setup excluded"},
-        "speedup_vs_one_by_one": (ninst / batch_s) / one_by_one,
+        "speedup_batched_fp32_vs_one_by_one": fp32_res["solves_per_s"] / one_by_one,
+        "speedup_batched_fp64_vs_one_by_one": fp64_res["solves_per_s"] / one_by_one,
+        "speedup_fp32_vs_fp64_batched": fp32_res["solves_per_s"] / fp64_res["solves_per_s"],
+        "note": "batched_* = all instances in one handle, one device Newton solve; oracle_fp64 = ||F(U_new)|| / "
+                "||F(U_n)|| per instance from the FP64 oracle (an instance that starts within FP64 resolution of "
+                "equilibrium counts when ||F|| is within 1e-11 of its error scale); converged = device residual "
+                "met 1e-8, ended_by_step_test_above_rtol = stopped by the step test above it",
     }
 
 
-def prisms_config3(ntri=20000, nlayers=40, steps=20, dt=20.0, rotation="vertical", oracle_every_step_max_cells=4_000_000,
-                   precond="lines"):
+def prisms_config3(ntri=200_000, nlayers=40, steps=20, dt=1.0, rotation="vertical", precond="clusters",
+                   max_cuts=4, attempt_max_it=20, oracle_threads=0):
     """Config 3: infiltration (1e-7 m/s through the top) into a dry soil on
-    Delaunay triangular prisms with per-cell full-tensor K, advanced ``steps``
-    backward-Euler steps of ``dt`` by the device Newton in the mixed form
-    (FP64 residual, FP32 Jacobian and inner solve).  Each step is also solved
-    from the same start in plain FP64 (FP64 Jacobian and inner solve), and the
-    FP64 oracle's residual of the mixed result relative to its residual at the
-    start of the step is reported per step (first and last step only above
-    ``oracle_every_step_max_cells``).
+    Delaunay triangular prisms with per-cell full-tensor K, ``steps``
+    intervals of ``dt`` advanced by the device Newton in the mixed form (FP64
+    residual, FP32 Jacobian and inner solve), and again, from the same start,
+    in plain FP64 (FP64 Jacobian and inner solve).
 
-    The step is short because MPFA-O on obtuse Delaunay triangles is not
-    monotone: where flux coefficients outweigh the accumulation term (which
-    scales with cell area / dt) the Jacobian has negative diagonal entries and
-    the line-preconditioned Krylov solve diverges.  Measured: 80 k cells
-    converge every step at dt = 600 s, 800 k cells at 20 s but not at 60 s."""
+    An interval is one backward-Euler step of dt; when Newton does not
+    converge (within ``attempt_max_it`` iterations) the interval is redone as
+    four steps of dt/4, recursively up to ``max_cuts`` levels: the cut of the
+    reference's time integrator (dt * 0.25 on a failed step,
+    src/tdyti.c:140-150).  Every backward-Euler step of the mixed run is
+    checked against the FP64 oracle: ||F(U_k+1)|| / ||F(U_k)|| with the
+    oracle's residual at that step's dt (threaded oracle)."""
     import torch
 
     import tdycore_gb300 as T
@@ -355,61 +398,88 @@ def prisms_config3(ntri=20000, nlayers=40, steps=20, dt=20.0, rotation="vertical
     log(f"config 3: {nc} cells, nnz {nnz}, setup {setup_s:.1f} s")
     o = Oracle(t.setup_view())
     dev = torch.device("cuda")
-    d = torch.tensor(U0, dtype=torch.float64, device=dev)
-    # warm-up: spmv autotune and graph capture of both arithmetic modes
+    # warm-up: spmv autotune and the inner-solve graphs of both arithmetic modes
     for fp32 in (True, False):
-        w = d.clone()
-        t.backward_euler_step_device(w, dt, fp32=fp32, precond=precond)
+        w = torch.tensor(U0, dtype=torch.float64, device=dev)
+        t.backward_euler_step_device(w, dt / 4 ** max_cuts, fp32=fp32, precond=precond, max_it=attempt_max_it)
     del w
-    every = nc <= oracle_every_step_max_cells
-    per_step, mixed_s, fp64_s = [], 0.0, 0.0
-    for s in range(steps):
-        Un = d.clone()
-        d64 = d.clone()
+
+    def advance(d, h, level, fp32, recs, check):
+        """One step of h, or four of h/4 (recursively) when it fails; appends
+        a record per backward-Euler step attempted; False if a step at the
+        deepest level fails."""
+        save = d.clone()
         torch.cuda.synchronize()
         ts = time.perf_counter()
-        st, its, rel = t.backward_euler_step_device(d, dt, fp32=True, precond=precond)
+        st, its, rel = t.backward_euler_step_device(d, h, fp32=fp32, precond=precond, max_it=attempt_max_it)
         torch.cuda.synchronize()
-        tm = time.perf_counter() - ts
-        ts = time.perf_counter()
-        st64, its64, rel64 = t.backward_euler_step_device(d64, dt, fp32=False, precond=precond)
-        torch.cuda.synchronize()
-        td = time.perf_counter() - ts
-        mixed_s += tm
-        fp64_s += td
-        diff = float(torch.max(torch.abs(d - d64) / torch.abs(d64)).item())
-        row = {"step": s + 1, "newton_mixed": int(its[0]), "newton_fp64": int(its64[0]),
-               "linear_mixed": st["linear_iterations"], "linear_fp64": st64["linear_iterations"],
-               "converged_mixed": st["converged"], "converged_fp64": st64["converged"],
-               "rel_residual_device": float(rel[0]), "mixed_s": tm, "fp64_s": td,
-               "max_rel_diff_mixed_vs_fp64": diff}
-        if every or s in (0, steps - 1):
-            un, u1 = Un.cpu().numpy(), d.cpu().numpy()
-            o.snes_presolve(un, dt)
-            f0 = np.linalg.norm(o.snes_function(un))
-            f1, m1 = o.snes_function(u1, with_mag=True)
-            row["oracle_rel_residual"] = float(np.linalg.norm(f1) / f0)
-            row["oracle_residual_over_scale"] = float(np.linalg.norm(f1) / np.linalg.norm(m1))
-        per_step.append(row)
-        log(f"config 3 step {s + 1}: {row}")
-    U = d.cpu().numpy()
+        ok = st["converged"] + st["step_converged"] == 1
+        rec = {"dt": h, "level": level, "converged": st["converged"] == 1,
+               "ended_by_step_test": st["step_converged"] == 1, "newton": int(its[0]),
+               "linear": st["linear_iterations"], "rel_residual_device": float(rel[0]),
+               "s": time.perf_counter() - ts}
+        if ok and check:
+            un, u1 = save.cpu().numpy(), d.cpu().numpy()
+            o.snes_presolve(un, h)
+            f0 = np.linalg.norm(o.snes_function_parallel(un, oracle_threads))
+            rec["oracle_rel_residual"] = float(np.linalg.norm(o.snes_function_parallel(u1, oracle_threads)) / f0)
+        recs.append(rec)
+        if ok:
+            return True
+        d.copy_(save)
+        if level == max_cuts:
+            return False
+        for _ in range(4):
+            if not advance(d, h / 4, level + 1, fp32, recs, check):
+                return False
+        return True
+
+    arms = {}
+    for name, fp32 in (("mixed", True), ("fp64", False)):
+        d = torch.tensor(U0, dtype=torch.float64, device=dev)
+        per_interval, total, completed = [], 0.0, 0
+        for k in range(steps):
+            recs = []
+            ok = advance(d, dt, 0, fp32, recs, check=fp32)
+            solve_s = sum(r["s"] for r in recs)  # device solves only (oracle checks excluded)
+            total += solve_s
+            done = [r for r in recs if r["converged"] or r["ended_by_step_test"]]
+            row = {"interval": k + 1, "ok": ok, "be_steps": len(done), "failed_attempts": len(recs) - len(done),
+                   "deepest_cut": max(r["level"] for r in recs), "newton": sum(r["newton"] for r in recs),
+                   "linear": sum(r["linear"] for r in recs), "solve_s": solve_s}
+            if fp32:
+                chk = [r["oracle_rel_residual"] for r in done if "oracle_rel_residual" in r]
+                row["oracle_rel_residual_max"] = max(chk) if chk else None
+                row["ended_by_step_test"] = sum(r["ended_by_step_test"] for r in done)
+            per_interval.append(row)
+            log(f"config 3 {name} interval {k + 1}: {row}")
+            if not ok:
+                break
+            completed += 1
+        arms[name] = {"intervals_completed": completed, "solve_s_total": total, "per_interval": per_interval,
+                      "U": d.cpu().numpy()}
+    m, f = arms["mixed"], arms["fp64"]
+    U = m.pop("U")
+    U64 = f.pop("U")
     t.destroy()
     T.options_clear()
-    checked = [r for r in per_step if "oracle_rel_residual" in r]
+    checked = [r["oracle_rel_residual_max"] for r in m["per_interval"] if r.get("oracle_rel_residual_max") is not None]
     return {
         "workload": info["workload"], "ncells": nc, "nnz_jacobian": nnz,
         "rotation": info["rotation"], "van_genuchten": info["van_genuchten"], "preconditioner": precond,
         "initial_pressure_pa": info["initial_pressure_pa"], "depth_m": info["depth_m"],
-        "top_flux_m_per_s": info["top_flux_m_per_s"], "dt_s": dt, "steps": steps, "setup_s": setup_s,
-        "mixed_s_total": mixed_s, "fp64_s_total": fp64_s, "speedup_mixed_vs_fp64": fp64_s / mixed_s,
-        "all_converged_mixed": all(r["converged_mixed"] == 1 for r in per_step),
-        "max_oracle_rel_residual": max(r["oracle_rel_residual"] for r in checked),
-        "max_rel_diff_mixed_vs_fp64": max(r["max_rel_diff_mixed_vs_fp64"] for r in per_step),
+        "top_flux_m_per_s": info["top_flux_m_per_s"], "dt_s": dt, "intervals": steps, "setup_s": setup_s,
+        "cut_policy": f"a failed step is redone as 4 steps of dt/4, up to {max_cuts} levels (src/tdyti.c:140-150); "
+                      f"an attempt fails after {attempt_max_it} Newton iterations",
+        "mixed": m, "fp64": f,
+        "all_intervals_completed_mixed": m["intervals_completed"] == steps,
+        "max_oracle_rel_residual": max(checked) if checked else None,
+        "speedup_mixed_vs_fp64": (f["solve_s_total"] / m["solve_s_total"]) if m["solve_s_total"] > 0 else None,
+        "final_max_rel_diff_mixed_vs_fp64": float(np.max(np.abs(U - U64) / np.abs(U64))),
         "pressure_range_pa_final": [float(U.min()), float(U.max())],
-        "per_step": per_step,
-        "note": "mixed = FP64 residual with FP32 Jacobian and inner solve; fp64 = the same step from the same "
-                "start with FP64 Jacobian and inner solve; oracle_rel_residual = ||F(U_mixed)|| / ||F(U_n)|| "
-                "from the FP64 CPU oracle",
+        "note": "mixed = FP64 residual with FP32 Jacobian and inner solve; fp64 = FP64 Jacobian and inner solve, "
+                "its own trajectory from the same start; oracle_rel_residual = ||F(U_k+1)|| / ||F(U_k)|| per "
+                "backward-Euler step of the mixed run from the FP64 CPU oracle (threaded)",
     }
 
 
@@ -567,8 +637,8 @@ def run_reference(args, rank):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": info["workload"], "ncells": view["ncells"], "form": "SNES F+J",
-                   "l2": "inputs larger than L2"},
+        "config": workload_config(info, view["ncells"], int(view["nnz"]), args.gpus),
+        "jacobian_arithmetic": "FP64",
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"{steps} full F+J evaluations of the {view['ncells']}-cell workload"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -647,23 +717,27 @@ def run_gpu(args, rank, world, local_rank):
     Rh = torch.empty(nc, dtype=torch.float64).pin_memory()
     Jh = torch.empty(nnz, dtype=torch.float64).pin_memory()
     Un, Rn, Jn = Uh.numpy(), Rh.numpy(), Jh.numpy()
-    t.presolve(Uprev)
-    for _ in range(2):
-        t.snes_function_jacobian(Un, Rn, Jn)
     e2e_steps = max(3, min(args.steps, 30))
-    if dist:
-        dist.barrier()
-    tt = time.perf_counter()
-    for _ in range(e2e_steps):
-        t.snes_function_jacobian(Un, Rn, Jn)
-    e2e_s = time.perf_counter() - tt
-    if dist:
-        te = torch.tensor([e2e_s], device=dev)
-        dist.all_reduce(te, op=dist.ReduceOp.MAX)
-        e2e_s = float(te.item())
-    e2e_value = world * nc * e2e_steps / e2e_s
 
-    # the same device loop with FP64 Jacobian products, for comparison
+    def end_to_end(tt_):
+        tt_.presolve(Uprev)
+        for _ in range(2):
+            tt_.snes_function_jacobian(Un, Rn, Jn)
+        if dist:
+            dist.barrier()
+        t_0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            tt_.snes_function_jacobian(Un, Rn, Jn)
+        el = time.perf_counter() - t_0
+        if dist:
+            te = torch.tensor([el], device=dev)
+            dist.all_reduce(te, op=dist.ReduceOp.MAX)
+            el = float(te.item())
+        return world * nc * e2e_steps / el
+
+    e2e_value = end_to_end(t)
+
+    # the same device loop and end-to-end call with FP64 Jacobian products
     R_main, J_main = dR.cpu().numpy(), dJ.cpu().numpy()
     alt = None
     if args.jacobian_arithmetic != "FP64":
@@ -691,7 +765,10 @@ def run_gpu(args, rank, world, local_rank):
         alt = {"jacobian_arithmetic": "FP64", "setup_s": info2["setup_s"],
                "value": world * nc * args.steps / (ms2 * 1e-3),
                "ms_per_step": ms2 / args.steps, "R": dR.cpu().numpy(), "J": dJ.cpu().numpy()}
+        alt["e2e"] = end_to_end(t2)
+        t2.presolve_device(dUp, stream=sp)  # the device loop's accumulation state for the FP64 parity check
         launches = t2.launches_per_evaluation()
+        t2.destroy()
     else:
         launches = t.launches_per_evaluation()
 
@@ -705,7 +782,6 @@ def run_gpu(args, rank, world, local_rank):
         vk_ms = kernel_ms.get("vertex_kernel", float("nan"))
         achieved = vb / (vk_ms * 1e-3) / 1e9
         balg = algorithmic_bytes(view)
-        flops = fp64_flops_per_eval(view)
         traffic = None
         tf = ROOT / "profiles" / "vertex_kernel_traffic.json"
         if tf.exists():
@@ -715,14 +791,17 @@ def run_gpu(args, rank, world, local_rank):
                 traffic = None
         o = make_oracle(view, Uprev)
         parity = {}
-        parity["R_err_over_scale"], parity[f"J_err_over_scale_{args.jacobian_arithmetic.lower()}"] = \
-            parity_full_size(o, U, R_main, J_main)
+        (parity["R_err_over_scale"], parity[f"J_err_over_scale_{args.jacobian_arithmetic.lower()}"],
+         parity["R_rel_l2"]) = parity_full_size(o, U, R_main, J_main)
         if alt is not None:
-            rr, jj = parity_full_size(o, U, alt["R"], alt["J"])
+            rr, jj, rl2 = parity_full_size(o, U, alt["R"], alt["J"])
             parity["R_err_over_scale_fp64_device_trans"] = rr
             parity["J_err_over_scale_fp64_device_trans"] = jj
-        parity["bars"] = {"R": 1e-12, "J": 1e-10}
+            parity["R_rel_l2_fp64_device_trans"] = rl2
+        parity["bars"] = {"R": 1e-12, "J": 1e-10, "R_rel_l2": 1e-12}
+        parity["state"] = "hydrostatic plus N(0, 5 kPa) noise (far from equilibrium); previous state N(0, 200 Pa) off"
         cpu_v, cores, n_cpu, cpu_s = cpu_baseline(o, U, budget_s=args.cpu_budget)
+        del o
         try:
             cfg1 = newton_config1()
         except Exception as e:  # reported, never fatal to the headline line
@@ -736,7 +815,8 @@ def run_gpu(args, rank, world, local_rank):
         cfg3 = None
         if args.prisms_triangles > 0:
             try:
-                cfg3 = prisms_config3(args.prisms_triangles, dt=args.prisms_dt, precond=args.prisms_precond)
+                cfg3 = prisms_config3(args.prisms_triangles, dt=args.prisms_dt, precond=args.prisms_precond,
+                                      steps=args.prisms_steps)
             except Exception as e:
                 cfg3 = {"error": repr(e)}
         if args.prisms_eval_triangles > 0:
@@ -755,20 +835,19 @@ def run_gpu(args, rank, world, local_rank):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": info["workload"], "ncells": nc, "nnz_jacobian": nnz, "form": "SNES F+J",
-                       "seed": info["seed"], "l2": "inputs larger than L2 (no flush)",
-                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                       "jacobian_arithmetic": args.jacobian_arithmetic},
+            "config": workload_config(info, nc, nnz, world),
+            "jacobian_arithmetic": args.jacobian_arithmetic,
             "roofline": {"bound": "hbm", "kernel": "vertex_kernel", "achieved": achieved, "peak": hbm_peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm_peak,
                          "traffic": traffic, "algorithmic_bytes_per_launch": vb,
-                         "avg_launch_ms": vk_ms},
+                         "algorithmic_bytes_formula": "8 * (sum_v R_v C_v + sum_v R_v + Nc): Trans, gravity "
+                                                      "term per row, cell pressures",
+                         "avg_launch_ms": vk_ms,
+                         "binding_roof": "FP64 pipe (see fp64.pipe_active_ncu)"},
             "roofline_evaluation": {"algorithmic_bytes": balg, "GBps": balg / (ms_per_step * 1e-3) / 1e9,
                                     "frac_hbm": balg / (ms_per_step * 1e-3) / 1e9 / hbm_peak,
                                     "bytes_per_cell": balg / nc},
-            "fp64": {"flops_per_eval": flops, "achieved_tflops": flops / (ms_per_step * 1e-3) / 1e12,
-                     "peak_tflops_probe": fp64_peak,
-                     "frac": (flops / (ms_per_step * 1e-3) / 1e12 / fp64_peak) if fp64_peak else None},
+            "fp64": {"peak_tflops_probe": fp64_peak, "pipe_active_ncu": fp64_pipe_from_profile(kernel_ms)},
             "kernel_ms": kernel_ms,
             "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": f"{n_cpu} full F+J evaluations ({cpu_s:.1f} s) of the same workload"},
@@ -788,8 +867,10 @@ def run_gpu(args, rank, world, local_rank):
         }
         if alt is not None:
             out["fp64_jacobian"] = {"value": alt["value"], "unit": UNIT, "ms_per_step": alt["ms_per_step"],
-                                    "note": "same device loop with -tdy_jacobian_arithmetic FP64 (and Trans "
-                                            "built on the device)"}
+                                    "e2e": {"value": alt["e2e"], "unit": UNIT, "h2d_bytes_per_step": 8 * nc,
+                                            "d2h_bytes_per_step": 8 * (nc + nnz), "steps": e2e_steps},
+                                    "note": "strict FP64: the same device loop and end-to-end call with "
+                                            "-tdy_jacobian_arithmetic FP64 (and Trans built on the device)"}
         print(json.dumps(out), flush=True)
     if dist:
         dist.barrier()
@@ -809,13 +890,16 @@ def main():
                     help="arithmetic of the Jacobian products at interior hexahedral vertices")
     ap.add_argument("--serve-requests", type=int, default=160,
                     help="requests of the serving measurement (0 skips it)")
-    ap.add_argument("--prisms-triangles", type=int, default=20000,
-                    help="surface triangles of the prism infiltration measurement (0 skips it)")
-    ap.add_argument("--prisms-dt", type=float, default=20.0,
+    ap.add_argument("--prisms-triangles", type=int, default=200000,
+                    help="surface triangles of the prism infiltration measurement (0 skips it; 200000 x 40 layers "
+                         "is the configuration's 8 M cells)")
+    ap.add_argument("--prisms-dt", type=float, default=1.0,
                     help="time step of the prism infiltration measurement (s)")
-    ap.add_argument("--prisms-precond", default="lines", choices=["lines", "clusters"],
+    ap.add_argument("--prisms-precond", default="clusters", choices=["lines", "clusters"],
                     help="inner-solve preconditioner of the prism infiltration measurement")
-    ap.add_argument("--prisms-eval-triangles", type=int, default=0,
+    ap.add_argument("--prisms-steps", type=int, default=20,
+                    help="backward-Euler steps of the prism infiltration measurement")
+    ap.add_argument("--prisms-eval-triangles", type=int, default=200000,
                     help="surface triangles of the mixed-form F+J evaluation on prisms with 3-D rotated K "
                          "(200000 is the full configuration; 0 skips it)")
     ap.add_argument("--batch-instances", type=int, default=4096,

@@ -228,7 +228,23 @@ typedef struct {
   int precond;         /* TDY_PRECOND_LINES (default) or TDY_PRECOND_CLUSTERS */
   double cluster_threshold; /* clusters: a coupling with |a_ij| >= threshold sqrt(|a_ii a_jj|)
                                joins cells i and j (default 0.05) */
+  int schedule;        /* inner-solve schedule with the line preconditioner: TDY_SCHEDULE_AUTO
+                          (default), _TILE or _BLOCK; every schedule gives the same bits */
+  int fp32_max_it;     /* with linear_fp32: Newton iterations with the FP32 inner solve, FP64 after
+                          (an instance still iterating then stalls on FP32 directions; default 8,
+                          negative: FP32 throughout) */
 } TDyNewtonOptions;
+/* Inner-solve schedules.  TILE: every kernel of a BiCGStab iteration runs over
+ * all cells of the batch, instances masked as they converge (one iteration is
+ * a CUDA graph).  BLOCK: one CTA per instance runs the instance's whole
+ * BiCGStab loop (CTAs take instances from a counter, largest first).  AUTO:
+ * an autotuner times the tile, block and split schedules (instances up to
+ * 4096, 16384 or 65536 cells on the block schedule, the rest on the tile
+ * schedule) on the first solve of a size class and keeps the fastest for the
+ * process.  The cluster preconditioner runs on the tile schedule. */
+#define TDY_SCHEDULE_AUTO 0
+#define TDY_SCHEDULE_TILE 1
+#define TDY_SCHEDULE_BLOCK 2
 /* Inner-solve preconditioners.  LINES: exact solves of the vertical lines of
  * the extruded blocks.  CLUSTERS: exact solves of the connected clusters of
  * strong couplings (up to 64 cells each; cells of larger clusters take their
@@ -248,6 +264,10 @@ typedef struct {
   int clusters;                 /* last inner solve: clusters of 2..64 cells factored */
   int cluster_cells;            /* last inner solve: cells in those clusters */
   int cluster_cells_diagonal;   /* last inner solve: cells of clusters larger than 64 (they take their diagonal) */
+  int block_instances;          /* last inner solve: instances on the block schedule */
+  long long block_max_cells;    /* last inner solve: the split (instances up to this many cells on the block
+                                   schedule; -1 none) */
+  int fp64_fallback;            /* 1 if Newton went past fp32_max_it and finished with FP64 inner solves */
 } TDyNewtonStats;
 TDyErrorCode TDyNewtonOptionsDefault(TDyNewtonOptions *o);
 TDyErrorCode TDyGetNumInstances(TDy tdy, int *n);
@@ -294,8 +314,9 @@ TDyErrorCode TDyPreSolveSNESSolverDevice(TDy tdy, const double *dU_prev, void *s
  * cudaFree may cause.  The caller passes inputs and outputs as device
  * pointers.  Meshes whose scratch would exceed the array (about 110,000
  * interior hexahedral vertices) are rejected with TDY_ERR_ARG_OUTOFRANGE.
- * The first call on a device looks up the array's device address, so make
- * that first call before capturing any stream.  All calls share the array:
+ * TDySetup looks up the array's device address once per device, so the call
+ * itself loads nothing and allocates nothing, even the first time.  All
+ * calls share the array:
  * calls that overlap on the GPU race and must be serialised by the caller.
  * This entry point has no counterpart in the reference. */
 TDyErrorCode TDyMPFAOSNESFunctionJacobianDeviceNoAlloc(TDy tdy, const double *dU, double *dR, double *dJ,

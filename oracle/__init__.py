@@ -59,6 +59,7 @@ def _load():
     lib.oracle_ts_ifunction.argtypes = [c_void_p, _dp, _dp, _dp, _dp]
     lib.oracle_ts_ijacobian.argtypes = [c_void_p, _dp, _dp, c_double, _dp, _dp]
     lib.oracle_snes_function_jacobian_parallel.argtypes = [c_void_p, _dp, _dp, _dp, c_int]
+    lib.oracle_snes_function_parallel.argtypes = [c_void_p, _dp, _dp, c_int]
     lib.oracle_get_state.argtypes = [c_void_p, _dp, _dp, _dp]
     lib.oracle_transient_variable.argtypes = [c_void_p, _dp, _dp, _dp]
     lib.oracle_tv_ifunction.argtypes = [c_void_p, _dp, _dp, _dp, _dp]
@@ -185,6 +186,14 @@ class Oracle:
         M = np.empty(2 * self.nc) if with_mag else None
         lib().oracle_dae_ifunction(self._ctx, _p(u), _p(ut), _p(R), _p(M) if with_mag else None)
         return (R, M) if with_mag else R
+
+    def snes_function_parallel(self, U, nthreads=0):
+        """The SNES residual with the vertex loop over colours on threads
+        (equal to snes_function up to the summation order)."""
+        u = np.ascontiguousarray(U, dtype=np.float64)
+        R = np.empty(self.nc)
+        lib().oracle_snes_function_parallel(self._ctx, _p(u), _p(R), nthreads)
+        return R
 
     def snes_function_jacobian_parallel(self, U, nthreads=0):
         u = np.ascontiguousarray(U, dtype=np.float64)

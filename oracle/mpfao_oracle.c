@@ -851,6 +851,40 @@ void oracle_tv_ijacobian(OracleCtx *c, const double *U, double shift, double *J,
 }
 
 /* ---------------------------------------------------------------------------
+ * Threaded residual only (per-step checks of long runs on large meshes): the
+ * state, boundary and Trans.P stages in parallel, the vertex loop over
+ * vertex colours.  The same terms as oracle_snes_function, summed in colour
+ * order, so the result differs from it only by rounding. */
+void oracle_snes_function_parallel(OracleCtx *c, const double *U, double *R, int nthreads) {
+  const OracleInput *in = &c->in;
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#else
+  (void)nthreads;
+#endif
+#pragma omp parallel num_threads(nthreads)
+  {
+#pragma omp for schedule(static)
+    for (int i = 0; i < c->nc; i++) R[i] = 0.0;
+#pragma omp for schedule(static)
+    for (int i = 0; i < c->nc; i++) update_state_range(c, U, i, i + 1);
+#pragma omp for schedule(static)
+    for (int b = 0; b < c->nb; b++) update_boundary_range(c, U, b, b + 1);
+#pragma omp for schedule(static)
+    for (int r = 0; r < c->nrows; r++) matmult_range(c, r, r + 1);
+    for (int col = 0; col < c->ncolors; col++) {
+#pragma omp for schedule(static)
+      for (int k = c->color_off[col]; k < c->color_off[col + 1]; k++) ifunction_vertex(c, c->color_vert[k], R, NULL);
+    }
+#pragma omp for schedule(static)
+    for (int i = 0; i < c->nc; i++) {
+      R[i] += snes_accum(c, i) - c->accum_prev[i];
+      R[i] -= in->source_sink[i];
+    }
+  }
+}
+
+/* ---------------------------------------------------------------------------
  * Threaded fused F+J for the CPU baseline. */
 void oracle_snes_function_jacobian_parallel(OracleCtx *c, const double *U, double *R, double *J, int nthreads) {
   const OracleInput *in = &c->in;

@@ -75,6 +75,7 @@ void oracle_tv_ijacobian(OracleCtx *ctx, const double *U, double shift, double *
 void oracle_dae_ifunction(OracleCtx *ctx, const double *U, const double *Ut, double *R, double *Rmag);
 /* Fused SNES F+J over all host threads, vertices processed by colour (used
  * for the CPU baseline timing; same arithmetic, different summation order). */
+void oracle_snes_function_parallel(OracleCtx *c, const double *U, double *R, int nthreads);
 void oracle_snes_function_jacobian_parallel(OracleCtx *ctx, const double *U, double *R, double *J, int nthreads);
 /* Per-cell state after the last evaluation (for diagnostics tests). */
 void oracle_get_state(OracleCtx *ctx, double *S, double *rho, double *Kr);

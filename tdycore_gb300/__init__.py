@@ -68,17 +68,19 @@ class TDyMPFAOSetupView(ctypes.Structure):
 class NewtonOptions(ctypes.Structure):
     _fields_ = [("rtol", c_double), ("atol", c_double), ("max_it", c_int), ("linear_fp32", c_int),
                 ("linear_rtol", c_double), ("linear_max_it", c_int), ("stol", c_double), ("precond", c_int),
-                ("cluster_threshold", c_double)]
+                ("cluster_threshold", c_double), ("schedule", c_int), ("fp32_max_it", c_int)]
 
 
 PRECOND_LINES, PRECOND_CLUSTERS = 0, 1
+SCHEDULE_AUTO, SCHEDULE_TILE, SCHEDULE_BLOCK = 0, 1, 2
 
 
 class NewtonStats(ctypes.Structure):
     _fields_ = [("newton_iterations", c_int), ("linear_iterations", c_longlong), ("converged", c_int),
                 ("ninstances", c_int), ("max_rel_residual", c_double), ("step_converged", c_int),
                 ("precond_used", c_int), ("clusters", c_int), ("cluster_cells", c_int),
-                ("cluster_cells_diagonal", c_int)]
+                ("cluster_cells_diagonal", c_int), ("block_instances", c_int), ("block_max_cells", c_longlong),
+                ("fp64_fallback", c_int)]
 
 
 def _sig(name, *args):
@@ -614,10 +616,13 @@ class TDy:
 
     def backward_euler_step_device(self, dU, dt, rtol=1e-8, atol=0.0, max_it=50, fp32=True, linear_rtol=1e-6,
                                    linear_max_it=400, stol=1e-8, stream=None, precond="lines",
-                                   cluster_threshold=0.05):
+                                   cluster_threshold=0.05, schedule="auto", fp32_max_it=8):
         """One backward-Euler step of every instance with the device Newton
         solver; dU (device float64 tensor, ncells) holds U_n and receives
-        U_{n+1}.  precond: "lines" or "clusters" (TDY_PRECOND_*).  Returns
+        U_{n+1}.  precond: "lines" or "clusters" (TDY_PRECOND_*); schedule:
+        "auto", "tile" or "block" (TDY_SCHEDULE_*, the same bits); with
+        fp32, inner solves switch to FP64 after fp32_max_it Newton iterations
+        (negative: never).  Returns
         (stats dict, per-instance Newton iterations, per-instance final
         ||F||/||F_0||)."""
         o = NewtonOptions()
@@ -626,6 +631,8 @@ class TDy:
         o.linear_rtol, o.linear_max_it, o.stol = linear_rtol, linear_max_it, stol
         o.precond = {"lines": PRECOND_LINES, "clusters": PRECOND_CLUSTERS}[precond]
         o.cluster_threshold = cluster_threshold
+        o.schedule = {"auto": SCHEDULE_AUTO, "tile": SCHEDULE_TILE, "block": SCHEDULE_BLOCK}[schedule]
+        o.fp32_max_it = fp32_max_it
         st = NewtonStats()
         ni = self.num_instances()
         its = np.zeros(ni, dtype=np.int32)

@@ -1036,6 +1036,8 @@ TDyErrorCode TDyNewtonOptionsDefault(TDyNewtonOptions *o) {
   o->stol = 1e-8;
   o->precond = TDY_PRECOND_LINES;
   o->cluster_threshold = 0.05;
+  o->schedule = TDY_SCHEDULE_AUTO;
+  o->fp32_max_it = 8;
   return 0;
 }
 TDyErrorCode TDyGetNumInstances(TDy tdy, int *n) {
@@ -1056,7 +1058,8 @@ TDyErrorCode TDyBackwardEulerStepDevice(TDy tdy, double dt, double *dU, const TD
   if (opt) o = *opt;
   if (o.max_it < 0 || o.linear_max_it < 1 || !(o.rtol >= 0.0) || !(o.linear_rtol > 0.0) ||
       (o.precond != TDY_PRECOND_LINES && o.precond != TDY_PRECOND_CLUSTERS) ||
-      (o.precond == TDY_PRECOND_CLUSTERS && !(o.cluster_threshold > 0.0)))
+      (o.precond == TDY_PRECOND_CLUSTERS && !(o.cluster_threshold > 0.0)) ||
+      (o.schedule != TDY_SCHEDULE_AUTO && o.schedule != TDY_SCHEDULE_TILE && o.schedule != TDY_SCHEDULE_BLOCK))
     return set_error(TDY_ERR_ARG_OUTOFRANGE, "TDyBackwardEulerStepDevice: invalid options");
   return device_be_solve(tdy, dt, dU, o, stats, inst_iterations, inst_rel_residual, stream);
 }

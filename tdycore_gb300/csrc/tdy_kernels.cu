@@ -44,6 +44,7 @@
 #include <type_traits>
 #include <vector>
 
+#include "tdy_arena.h"
 #include "tdy_device.h"
 #include "tdy_ff.h"
 
@@ -540,7 +541,7 @@ __device__ __forceinline__ void canon_vertex(const DevArgs &a, int block) {
       // entries of rows upwinded from nearly dry cells (kr ~ 1e-30 and
       // below) keep full relative accuracy next to O(1) entries.
       double wk[3], es[3], en[3], Tk[3][8];
-      int bw[3], bt[3][8], mb[8];
+      int bw[3], mb[8];
 #pragma unroll
       for (int j = 0; j < 8; j++) mb[j] = 0;
 #pragma unroll
@@ -556,9 +557,8 @@ __device__ __forceinline__ void canon_vertex(const DevArgs &a, int block) {
 #pragma unroll
         for (int j = 0; j < 8; j++) {
           Tk[k][j] = T[(j ^ c) * P];
-          bt[k][j] = d_bexp(Tk[k][j]);
           // biased exponent of |w T| (a zero factor gives a negligible value)
-          mb[j] = max(mb[j], bw[k] + bt[k][j] - 1023);
+          mb[j] = max(mb[j], bw[k] + d_bexp(Tk[k][j]) - 1023);
         }
         mb[0] = max(mb[0], d_bexp(es[k]));
         mb[1 << k] = max(mb[1 << k], d_bexp(en[k]));
@@ -579,7 +579,8 @@ __device__ __forceinline__ void canon_vertex(const DevArgs &a, int block) {
           nf = ff_neg(nf);
         }
 #pragma unroll
-        for (int j = 0; j < 8; j++) ff_acc(acc[j], ff_mul(wf, ff_split_scaled(Tk[k][j], bt[k][j], bw[k] - mb[j])));
+        for (int j = 0; j < 8; j++)
+          ff_acc(acc[j], ff_mul(wf, ff_split_scaled(Tk[k][j], d_bexp(Tk[k][j]), bw[k] - mb[j])));
         ff_acc(acc[0], ef);
         ff_acc(acc[1 << k], nf);
       }
@@ -818,6 +819,7 @@ __global__ void __launch_bounds__(128) generic_vertex_kernel(DevArgs a) { generi
 // gather program; each warp stages its rows in shared memory and writes them
 // with coalesced stores.  Both sum the vertices in the cell's corner order, so
 // a cell gets the same bits on either path.
+
 __device__ __forceinline__ void struct_cell(const DevArgs &a, int block) {
   extern __shared__ double rowbuf[];
   const int sidx = block * blockDim.x + threadIdx.x;
@@ -907,9 +909,9 @@ __device__ __forceinline__ void generic_cell_thread(const DevArgs &a, int block)
     int diag = -1;
     for (int k = k0; k < k1; k++) {
       const int nint = a.cv_nint[k], stride = a.cv_stride[k];
-      const double *blk = a.scratch + a.cv_jbase[k];
+      const long long jb = a.cv_jbase[k];
       const unsigned char *sl = a.cv_slots + a.cv_slot_off[k];
-      for (int b = 0; b < nint; b++) row[sl[b]] += blk[(long long)b * stride];
+      for (int b = 0; b < nint; b++) row[sl[b]] += a.scratch[jb + (long long)b * stride];
       diag = sl[a.cv_local[k]];
     }
     if (diag >= 0) row[diag] += a.jdiag[i];
@@ -952,9 +954,9 @@ __device__ __forceinline__ void generic_cell_warp(const DevArgs &a, int block) {
   int diag = -1;
   for (int k = k0; k < k1; k++) {
     const int nint = a.cv_nint[k], stride = a.cv_stride[k];
-    const double *blk = a.scratch + a.cv_jbase[k];
+    const long long jb = a.cv_jbase[k];
     const unsigned char *sl = a.cv_slots + a.cv_slot_off[k];
-    for (int b = hl; b < nint; b += 16) row[sl[b]] += blk[(long long)b * stride];
+    for (int b = hl; b < nint; b += 16) row[sl[b]] += a.scratch[jb + (long long)b * stride];
     diag = sl[a.cv_local[k]];
     __syncwarp(mask);
   }
@@ -1018,14 +1020,7 @@ static int dalloc(DeviceState *d, T **p, size_t n) {
   return 0;
 }
 
-// (h must stay alive until d->stream is synchronised)
-template <class T>
-static int dupload(DeviceState *d, T **p, const std::vector<T> &h) {
-  int ierr = dalloc(d, p, h.size());
-  if (ierr) return ierr;
-  if (!h.empty()) CUDA_TRY(cudaMemcpyAsync(*p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, d->stream));
-  return 0;
-}
+static int pool_event(cudaEvent_t *ev);
 
 // Records that a caller's stream enqueued work on this handle.
 static int note_stream(DeviceState *d, cudaStream_t st) {
@@ -1036,7 +1031,8 @@ static int note_stream(DeviceState *d, cudaStream_t st) {
       return 0;
     }
   cudaEvent_t e;
-  CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  int ierr = pool_event(&e);
+  if (ierr) return ierr;
   d->user_streams.emplace_back(st, e);
   CUDA_TRY(cudaEventRecord(e, st));
   return 0;
@@ -1113,6 +1109,54 @@ static int cell_smem_optin(int dev, size_t bytes) {
   return 0;
 }
 
+// Streams and events of handles come from per-device pools and go back to
+// them when the handle is destroyed (after their work has completed):
+// creating and destroying them waits on the driver, and a server sets up and
+// destroys handles on many threads at once.
+static std::vector<cudaStream_t> g_stream_pool[kMaxDevices];
+static std::vector<cudaEvent_t> g_event_pool[kMaxDevices];
+
+static int pool_device(int *dev) {
+  CUDA_TRY(cudaGetDevice(dev));
+  if (*dev < 0 || *dev >= kMaxDevices) return set_error(TDY_ERR_SUP, "device ordinal %d not supported", *dev);
+  return 0;
+}
+static int pool_stream(cudaStream_t *st) {
+  int dev, ierr;
+  if ((ierr = pool_device(&dev))) return ierr;
+  {
+    std::lock_guard<std::mutex> lk(g_dev_mutex);
+    if (!g_stream_pool[dev].empty()) {
+      *st = g_stream_pool[dev].back();
+      g_stream_pool[dev].pop_back();
+      return 0;
+    }
+  }
+  CUDA_TRY(cudaStreamCreateWithFlags(st, cudaStreamNonBlocking));
+  return 0;
+}
+static int pool_event(cudaEvent_t *ev) {
+  int dev, ierr;
+  if ((ierr = pool_device(&dev))) return ierr;
+  {
+    std::lock_guard<std::mutex> lk(g_dev_mutex);
+    if (!g_event_pool[dev].empty()) {
+      *ev = g_event_pool[dev].back();
+      g_event_pool[dev].pop_back();
+      return 0;
+    }
+  }
+  CUDA_TRY(cudaEventCreateWithFlags(ev, cudaEventDisableTiming));
+  return 0;
+}
+// (dev: the device the stream or event was made on; its work has completed)
+static void pool_release(int dev, cudaStream_t st, cudaEvent_t ev) {
+  if (dev < 0 || dev >= kMaxDevices) return;
+  std::lock_guard<std::mutex> lk(g_dev_mutex);
+  if (st) g_stream_pool[dev].push_back(st);
+  if (ev) g_event_pool[dev].push_back(ev);
+}
+
 int device_setup(_p_TDy *t) {
   const Mesh &m = t->mesh;
   const MPFAOSetup &s = t->setup;
@@ -1127,7 +1171,8 @@ int device_setup(_p_TDy *t) {
   DeviceState *d = new DeviceState();
   t->dev = d;
   CUDA_TRY(cudaGetDevice(&d->device));
-  CUDA_TRY(cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking));
+  int ierr = 0;
+  if ((ierr = pool_stream(&d->stream))) return ierr;
   DevArgs &a = d->a;
   memset(&a, 0, sizeof(a));
   a.nc = m.nc;
@@ -1137,153 +1182,141 @@ int device_setup(_p_TDy *t) {
   a.rho_type = t->opt.rho_type;
   a.mu_type = t->opt.mu_type;
   const int next = m.nc + m.nb;
-  int ierr = 0;
-#define UP(ptr, vec)                                                           \
-  do {                                                                         \
-    decltype(vec) const &v_ = (vec);                                           \
-    using E_ = typename std::remove_const<typename std::remove_reference<decltype(v_[0])>::type>::type; \
-    E_ *p_;                                                                    \
-    if ((ierr = dupload(d, &p_, v_))) return ierr;                             \
-    ptr = p_;                                                                  \
-  } while (0)
-  UP(a.vol, m.cell_vol);
-  UP(a.poro, t->mat.porosity);
-  UP(a.Sr, t->mat.Sr);
-  UP(a.sat_param, t->mat.sat_param);
-  UP(a.rp_param, t->mat.relperm_param);
-  UP(a.ss, t->mat.source_sink);
-  UP(a.sat_type, t->mat.sat_type);
-  UP(a.rp_type, t->mat.relperm_type);
-  UP(a.lam_sat, t->mat.lam_sat);
+  // every array of the handle in one allocation, uploaded with one copy
+  Arena ar;
+  ar.up(&a.vol, m.cell_vol);
+  ar.up(&a.poro, t->mat.porosity);
+  ar.up(&a.Sr, t->mat.Sr);
+  ar.up(&a.sat_param, t->mat.sat_param);
+  ar.up(&a.rp_param, t->mat.relperm_param);
+  ar.up(&a.ss, t->mat.source_sink);
+  ar.up(&a.sat_type, t->mat.sat_type);
+  ar.up(&a.rp_type, t->mat.relperm_type);
+  ar.up(&a.lam_sat, t->mat.lam_sat);
   a.vis = t->mat.vis;
   std::vector<int> bnd_cell(m.nb);
   for (int b = 0; b < m.nb; b++) bnd_cell[b] = m.face_cell1[m.bnd_face[b]];
-  UP(a.bnd_cell, bnd_cell);
-  UP(a.bnd_type, t->bnd.type);
-  UP(a.bnd_has, t->bnd.has_value);
-  UP(a.bnd_val, t->bnd.value);
-  UP(a.bnd_rho, t->bnd.rho);
-  UP(a.bnd_vis, t->bnd.vis);
+  ar.up(&a.bnd_cell, bnd_cell);
+  ar.up(&a.bnd_type, t->bnd.type);
+  ar.up(&a.bnd_has, t->bnd.has_value);
+  ar.up(&a.bnd_val, t->bnd.value);
+  ar.up(&a.bnd_rho, t->bnd.rho);
+  ar.up(&a.bnd_vis, t->bnd.vis);
   std::vector<int> fup(m.nf), fdn(m.nf);
   for (int f = 0; f < m.nf; f++) {
     int u = m.face_cell0[f], w = m.face_cell1[f];
     fup[f] = u >= 0 ? u : m.nc + (-u - 1);
     fdn[f] = w >= 0 ? w : m.nc + (-w - 1);
   }
-  UP(a.f_up, fup);
-  UP(a.f_dn, fdn);
-  UP(a.G, s.gravdis);
+  ar.up(&a.f_up, fup);
+  ar.up(&a.f_dn, fdn);
+  ar.up(&a.G, s.gravdis);
   a.nC = s.nC;
   a.vc0 = 0;
   a.vc1 = s.nC;
   a.nCpad = s.nCpad;
-  if (t->opt.setup_on_device) {
-    double *tc;
-    if ((ierr = dalloc(d, &tc, 96 * (size_t)s.nCpad))) return ierr;
-    a.Tc = tc;
-  } else {
-    UP(a.Tc, s.Tc);
-  }
+  if (t->opt.setup_on_device)
+    ar.work(&a.Tc, 96 * (size_t)s.nCpad);
+  else
+    ar.up(&a.Tc, s.Tc);
   a.jac_ff = t->opt.jacobian_arithmetic == JACOBIAN_DOUBLE_FLOAT;
-  UP(a.cellc, s.cellc);
-  UP(a.facec, s.facec);
-  if (t->opt.setup_on_device &&
-      (ierr = device_canon_trans(t, a.cellc, a.facec, const_cast<double *>(a.Tc), d->stream)))
-    return ierr;
+  ar.up(&a.cellc, s.cellc);
+  ar.up(&a.facec, s.facec);
   a.ngen = (int)s.gen_vertex.size();
   // per row: w, E_up, E_dn, flux (doubles) and the two local-cell indices
   // (ints); per local cell: a row count and a list of kGenCellRows rows (bytes)
   a.gen_warp_doubles = 5 * TDY_MAX_ROWS + (TDY_MAX_NINT * (1 + kGenCellRows) + 7) / 8;
-  UP(a.gen_vertex, s.gen_vertex);
-  UP(a.v_row_off, s.v_row_off);
-  UP(a.v_col_off, s.v_col_off);
-  UP(a.v_nint, s.v_nint);
-  UP(a.v_trans_off, s.v_trans_off);
-  UP(a.v_jv_off, s.v_jv_off);
-  UP(a.row_face, s.row_face);
-  UP(a.row_lup, s.row_lup);
-  UP(a.row_ldn, s.row_ldn);
-  UP(a.col_ext, s.col_ext);
-  UP(a.trans, s.trans);
-  UP(a.rowptr, s.rowptr);
-  UP(a.cv_off, s.cv_off);
-  UP(a.cv_jbase, s.cv_jbase);
-  UP(a.cv_rbase, s.cv_rbase);
-  UP(a.cv_stride, s.cv_stride);
-  UP(a.cv_nint, s.cv_nint);
-  UP(a.cv_local, s.cv_local);
-  UP(a.cv_slot_off, s.cv_slot_off);
-  UP(a.cv_slots, s.cv_slots);
+  ar.up(&a.gen_vertex, s.gen_vertex);
+  ar.up(&a.v_row_off, s.v_row_off);
+  ar.up(&a.v_col_off, s.v_col_off);
+  ar.up(&a.v_nint, s.v_nint);
+  ar.up(&a.v_trans_off, s.v_trans_off);
+  ar.up(&a.v_jv_off, s.v_jv_off);
+  ar.up(&a.row_face, s.row_face);
+  ar.up(&a.row_lup, s.row_lup);
+  ar.up(&a.row_ldn, s.row_ldn);
+  ar.up(&a.col_ext, s.col_ext);
+  ar.up(&a.trans, s.trans);
+  ar.up(&a.rowptr, s.rowptr);
+  ar.up(&a.cv_off, s.cv_off);
+  ar.up(&a.cv_jbase, s.cv_jbase);
+  ar.up(&a.cv_rbase, s.cv_rbase);
+  ar.up(&a.cv_stride, s.cv_stride);
+  ar.up(&a.cv_nint, s.cv_nint);
+  ar.up(&a.cv_local, s.cv_local);
+  ar.up(&a.cv_slot_off, s.cv_slot_off);
+  ar.up(&a.cv_slots, s.cv_slots);
   a.max_row_nnz = s.max_row_nnz;
   a.nS = s.nS;
   a.nSpad = s.nSpad;
   a.ngc = (int)s.gc_cells.size();
-  UP(a.sc_cells, s.sc_cells);
-  UP(a.sc_vc, s.sc_vc);
-  UP(a.gc_cells, s.gc_cells);
-#undef UP
-  double *p;
-  if ((ierr = dalloc(d, &a.P, next))) return ierr;
-  if ((ierr = dalloc(d, &a.hr, next))) return ierr;
-  if ((ierr = dalloc(d, &a.hdr, next))) return ierr;
-  if ((ierr = dalloc(d, &a.lam, next))) return ierr;
-  if ((ierr = dalloc(d, &a.dlam, next))) return ierr;
-  if ((ierr = dalloc(d, &a.seep, next))) return ierr;
-  if ((ierr = dalloc(d, &a.acc_a, m.nc))) return ierr;
-  if ((ierr = dalloc(d, &a.acc_b, m.nc))) return ierr;
-  if ((ierr = dalloc(d, &a.jdiag, m.nc))) return ierr;
-  if ((ierr = dalloc(d, &p, m.nc))) return ierr;
-  CUDA_TRY(cudaMemsetAsync(p, 0, sizeof(double) * m.nc, d->stream));
-  a.accum_prev = p;
-  if ((ierr = dalloc(d, &a.scratch, (size_t)s.scratch_size))) return ierr;
+  ar.up(&a.sc_cells, s.sc_cells);
+  ar.up(&a.sc_vc, s.sc_vc);
+  ar.up(&a.gc_cells, s.gc_cells);
+  ar.work(&a.P, next);
+  ar.work(&a.hr, next);
+  ar.work(&a.hdr, next);
+  ar.work(&a.lam, next);
+  ar.work(&a.dlam, next);
+  ar.work(&a.seep, next);
+  ar.work(&a.acc_a, m.nc);
+  ar.work(&a.acc_b, m.nc);
+  ar.work(&a.jdiag, m.nc);
+  double *accum_prev = nullptr;
+  ar.work(&accum_prev, m.nc);
+  ar.work(&a.scratch, (size_t)s.scratch_size);
   d->nnz = (int)s.colidx.size();
-  if ((ierr = dalloc(d, &d->dU, m.nc))) return ierr;
-  if ((ierr = dalloc(d, &d->dUt, m.nc))) return ierr;
-  if ((ierr = dalloc(d, &d->dR, m.nc))) return ierr;
-  if ((ierr = dalloc(d, &d->dJ, d->nnz))) return ierr;
-  if ((ierr = dalloc(d, &d->diagS, m.nc))) return ierr;
-  if ((ierr = dalloc(d, &d->diagMass, m.nc))) return ierr;
-  build_slabs(t, d);
-  if (d->slabs.size() > 1) {
-    CUDA_TRY(cudaStreamCreateWithFlags(&d->copy_stream, cudaStreamNonBlocking));
-    d->slab_ev.assign(d->slabs.size(), nullptr);
-    for (cudaEvent_t &e : d->slab_ev) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-  }
+  ar.work(&d->dU, m.nc);
+  ar.work(&d->dUt, m.nc);
+  ar.work(&d->dR, m.nc);
+  ar.work(&d->dJ, d->nnz);
+  ar.work(&d->diagS, m.nc);
+  ar.work(&d->diagMass, m.nc);
+  if ((ierr = ar.commit(d->stream))) return ierr;
+  d->allocs.push_back(ar.base);
+  CUDA_TRY(cudaMemsetAsync(accum_prev, 0, sizeof(double) * m.nc, d->stream));
+  a.accum_prev = accum_prev;
+  if (t->opt.setup_on_device &&
+      (ierr = device_canon_trans(t, a.cellc, a.facec, const_cast<double *>(a.Tc), d->stream)))
+    return ierr;
+  build_slabs(t, d);  // their copy stream and events are taken on first use
   if ((ierr = cell_smem_optin(d->device, cell_smem_bytes(a, cell_warp_form(a))))) return ierr;
   if ((ierr = noalloc_resolve(d->device))) return ierr;
-  CUDA_TRY(cudaEventCreateWithFlags(&d->noalloc_ev, cudaEventDisableTiming));
+  if ((ierr = pool_event(&d->noalloc_ev))) return ierr;
   // the uploads (and the device-built Trans) are complete before any other
-  // stream uses them; only this handle's stream is waited for
+  // stream uses them, and the staging buffer and host vectors above outlive
+  // them; only this handle's stream is waited for
   CUDA_TRY(cudaStreamSynchronize(d->stream));
   return 0;
 }
 
 // Waits for the work this handle has in flight (its own streams and the
-// callers' streams it has seen), then frees its memory stream-ordered: no
-// device-wide synchronisation, so other handles keep running.
+// callers' streams it has seen), frees its memory stream-ordered (no
+// device-wide synchronisation, so other handles keep running) and returns its
+// streams and events to the pools.
 void device_destroy(_p_TDy *t) {
   DeviceState *d = t->dev;
   if (!d) return;
   if (d->stream) cudaStreamSynchronize(d->stream);
   for (auto &u : d->user_streams) {
     cudaEventSynchronize(u.second);
-    cudaEventDestroy(u.second);
+    pool_release(d->device, nullptr, u.second);
   }
   if (d->noalloc_ev) {
     cudaEventSynchronize(d->noalloc_ev);
-    cudaEventDestroy(d->noalloc_ev);
+    pool_release(d->device, nullptr, d->noalloc_ev);
   }
   for (int k = 0; k < 4; k++)
     if (d->ev[k]) cudaEventDestroy(d->ev[k]);
   if (d->copy_stream) {
     cudaStreamSynchronize(d->copy_stream);
-    cudaStreamDestroy(d->copy_stream);
+    pool_release(d->device, d->copy_stream, nullptr);
   }
-  for (cudaEvent_t e : d->slab_ev) cudaEventDestroy(e);
+  for (cudaEvent_t e : d->slab_ev) pool_release(d->device, nullptr, e);
   if (d->stream) {
     for (void *p : d->allocs) dmem_free(p, d->stream);
     cudaStreamSynchronize(d->stream);
-    cudaStreamDestroy(d->stream);
+    pool_release(d->device, d->stream, nullptr);
   }
   delete d;
   t->dev = nullptr;
@@ -1575,6 +1608,12 @@ int device_eval_host(_p_TDy *t, int form, double time, const double *U, const do
     DevArgs a;
     int ierr = eval_args(t, form, d->dU, Ut ? d->dUt : nullptr, shift, R ? d->dR : nullptr, d->dJ, &a);
     if (ierr) return ierr;
+    if (!d->copy_stream) {  // first host-pointer Jacobian call of this handle
+      if ((ierr = pool_stream(&d->copy_stream))) return ierr;
+      d->slab_ev.assign(d->slabs.size(), nullptr);
+      for (cudaEvent_t &e : d->slab_ev)
+        if ((ierr = pool_event(&e))) return ierr;
+    }
     const bool vw = vertex_warp_form(a), cw = cell_warp_form(a);
     if ((ierr = launch_state(a, d->stream))) return ierr;
     for (size_t k = 0; k < d->slabs.size(); k++) {

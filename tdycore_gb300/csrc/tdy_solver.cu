@@ -22,6 +22,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -29,6 +31,7 @@
 #include <utility>
 #include <vector>
 
+#include "tdy_arena.h"
 #include "tdy_device.h"
 
 namespace tdy {
@@ -129,6 +132,14 @@ struct SolverState {
   std::vector<int> h_lab, h_cnt, h_id, h_fill, h_loc, h_mem, h_off;
   std::vector<long long> h_luoff;
   Krylov k32, k64;
+  // schedules of the line-preconditioned inner solve (block: one CTA per
+  // instance; tile: the batch-wide graph): instances with at most
+  // block_max_cells cells take the block schedule (-2: not chosen yet)
+  int *inst_line_off = nullptr, *block_inst = nullptr, *block_mask = nullptr, *ticket = nullptr;
+  std::vector<int> h_inst_line_off, h_order;  // h_order: instances by size, largest first
+  long long block_max_cells = -2, mask_for = -3;
+  int n_block = 0, n_tile = 0;
+  std::vector<double> tune_ms;  // measured candidates of the last tuning (ms per linear solve)
   // device memory: stream-ordered on the handle's stream (allocated there and
   // synchronised at init; freed there when the solver is destroyed, after
   // every solve has synchronised its stream)
@@ -165,6 +176,41 @@ int sup(SolverState *s, T **p, const std::vector<T> &h) {
 
 // ---------------------------------------------------------------------------
 // kernels
+//
+// Two schedules run the BiCGStab iterations: "tile" (every kernel over all
+// cells of the batch, instances masked as they converge; one iteration is a
+// graph) and "block" (one CTA per instance runs its whole Krylov loop, see
+// bicgstab_block_kernel).  Both perform every floating-point operation of an
+// instance in the same order with explicit roundings (the element operations
+// below, the chunked reductions, the per-row lane split of the product), so
+// an instance gets the same bits from either schedule.
+
+__device__ __forceinline__ float e_fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double e_fma(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float e_mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double e_mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float e_add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double e_add(double a, double b) { return __dadd_rn(a, b); }
+
+// p = r + beta (p - omega v)
+template <class T>
+__device__ __forceinline__ T op_p(T r, T p, T v, T beta, T omega) {
+  return e_fma(beta, e_fma(-omega, v, p), r);
+}
+// y += alpha ph (+ omega sh)
+template <class T>
+__device__ __forceinline__ T op_y(T y, T ph, T alpha) {
+  return e_fma(alpha, ph, y);
+}
+template <class T>
+__device__ __forceinline__ T op_y2(T y, T ph, T sh, T alpha, T omega) {
+  return e_fma(omega, sh, e_fma(alpha, ph, y));
+}
+// the per-cell terms of the chunked dot products, in FP64
+template <class TA, class TB>
+__device__ __forceinline__ double op_dot(double acc, TA a, TB b) {
+  return __fma_rn((double)a, (double)b, acc);
+}
 
 template <class T>
 __global__ void cast_kernel(long long n, const double *a, T *b) {
@@ -186,8 +232,8 @@ __global__ void __launch_bounds__(256) chunk_dot_kernel(const int *chunk_off, co
   const int i0 = chunk_off[ch], i1 = chunk_off[ch + 1];
   double acc = 0.0, acc2 = 0.0;
   for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-    acc += (double)a[i] * (double)b[i];
-    if (c) acc2 += (double)c[i] * (double)d[i];
+    acc = op_dot(acc, a[i], b[i]);
+    if (c) acc2 = op_dot(acc2, c[i], d[i]);
   }
   sh[0][threadIdx.x] = acc;
   sh[1][threadIdx.x] = acc2;
@@ -226,9 +272,9 @@ __global__ void __launch_bounds__(256) spmv_kernel(int n, const int *rowptr, con
   const int row = (int)(gt / TPR), lane = (int)(gt % TPR);
   T acc = 0;
   if (row < n)
-    for (int k = rowptr[row] + lane; k < rowptr[row + 1]; k += TPR) acc += A[k] * x[colidx[k]];
+    for (int k = rowptr[row] + lane; k < rowptr[row + 1]; k += TPR) acc = e_fma(A[k], x[colidx[k]], acc);
 #pragma unroll
-  for (int o = TPR / 2; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o, TPR);
+  for (int o = TPR / 2; o > 0; o >>= 1) acc = e_add(acc, __shfl_down_sync(0xffffffffu, acc, o, TPR));
   if (row < n && lane == 0) y[row] = acc;
 }
 
@@ -251,25 +297,30 @@ __global__ void line_factor_kernel(int nlines, const int *line_off, const int *p
   }
 }
 
-// out = (line-tridiagonal)^-1 in
+// out = (line-tridiagonal)^-1 in, line l
 template <class T>
-__global__ void line_solve_kernel(int nlines, const int *line_off, const int *line_cells, const T *la, const T *lcp,
-                                  const T *linv, const T *in, T *out) {
-  const int l = blockIdx.x * blockDim.x + threadIdx.x;
-  if (l >= nlines) return;
+__device__ __forceinline__ void line_solve_one(int l, const int *line_off, const int *line_cells, const T *la,
+                                               const T *lcp, const T *linv, const T *in, T *out) {
   const int k0 = line_off[l], k1 = line_off[l + 1];
   T prev = 0;
   for (int k = k0; k < k1; k++) {
     const int i = line_cells[k];
-    prev = (in[i] - la[k] * prev) * linv[k];
+    prev = e_mul(e_fma(-la[k], prev, in[i]), linv[k]);
     out[i] = prev;
   }
   T next = 0;
   for (int k = k1 - 1; k >= k0; k--) {
     const int i = line_cells[k];
-    next = out[i] - lcp[k] * next;
+    next = e_fma(-lcp[k], next, out[i]);
     out[i] = next;
   }
+}
+template <class T>
+__global__ void line_solve_kernel(int nlines, const int *line_off, const int *line_cells, const T *la, const T *lcp,
+                                  const T *linv, const T *in, T *out) {
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= nlines) return;
+  line_solve_one(l, line_off, line_cells, la, lcp, linv, in, out);
 }
 
 template <class T>
@@ -286,14 +337,16 @@ __global__ void init_kernel(int n, const int *cell_seg, const int *active, const
   y[i] = 0;
 }
 
-__global__ void init_scalars_kernel(int nseg, const int *newt_active, int *lin_active, int *lin_its, double *scal) {
+// (instances on the block schedule stay inactive in the tile iterations)
+__global__ void init_scalars_kernel(int nseg, const int *newt_active, const int *block_mask, int *lin_active,
+                                    int *lin_its, double *scal) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nseg) return;
   scal[S_RHO * nseg + s] = 1.0;
   scal[S_ALPHA * nseg + s] = 1.0;
   scal[S_OMEGA * nseg + s] = 1.0;
   scal[S_HALF * nseg + s] = 0.0;
-  lin_active[s] = newt_active[s] && scal[S_BNORM2 * nseg + s] > 0.0;
+  lin_active[s] = newt_active[s] && scal[S_BNORM2 * nseg + s] > 0.0 && !block_mask[s];
 }
 
 // after rho_new = (r0, r) in T1
@@ -350,7 +403,7 @@ __global__ void p_update_kernel(int n, const int *cs, const int *act, const doub
   const int s = cs[i];
   if (!act[s]) return;
   const T beta = (T)sc[S_BETA * nseg + s], omega = (T)sc[S_OMEGA * nseg + s];
-  p[i] = r[i] + beta * (p[i] - omega * v[i]);
+  p[i] = op_p(r[i], p[i], v[i], beta, omega);
 }
 template <class T>
 __global__ void s_update_kernel(int n, const int *cs, const int *act, const double *sc, int nseg, const T *r, const T *v,
@@ -359,7 +412,7 @@ __global__ void s_update_kernel(int n, const int *cs, const int *act, const doub
   if (i >= n) return;
   const int s = cs[i];
   if (!act[s]) return;
-  sv[i] = r[i] - (T)sc[S_ALPHA * nseg + s] * v[i];
+  sv[i] = e_fma(-(T)sc[S_ALPHA * nseg + s], v[i], r[i]);
 }
 template <class T>
 __global__ void xr_update_kernel(int n, const int *cs, const int *act, const double *sc, int nseg, const T *ph,
@@ -370,12 +423,171 @@ __global__ void xr_update_kernel(int n, const int *cs, const int *act, const dou
   if (!act[s]) return;
   const T alpha = (T)sc[S_ALPHA * nseg + s];
   if (sc[S_HALF * nseg + s] != 0.0) {
-    y[i] += alpha * ph[i];
+    y[i] = op_y(y[i], ph[i], alpha);
     return;
   }
   const T omega = (T)sc[S_OMEGA * nseg + s];
-  y[i] += alpha * ph[i] + omega * sh[i];
-  r[i] = sv[i] - omega * tv[i];
+  y[i] = op_y2(y[i], ph[i], sh[i], alpha, omega);
+  r[i] = e_fma(-omega, tv[i], sv[i]);
+}
+
+// ---------------------------------------------------------------------------
+// Block schedule: one CTA of kBlockThreads threads per instance runs the
+// instance's whole BiCGStab loop with the line preconditioner, performing the
+// tile schedule's operations in the tile schedule's order (reductions in
+// kChunk-cell chunks with the same per-chunk tree and in-order chunk sum, the
+// product's rows split over TPR lanes the same way), so the two schedules
+// give the same bits.  CTAs take instances from a ticket counter, largest
+// first; an instance's result does not depend on which CTA takes it.
+constexpr int kBlockThreads = 256;
+static_assert(kBlockThreads == 256, "the block schedule's reductions mirror the 256-thread chunk reductions");
+
+template <class T>
+struct BlockSolve {
+  int ninst;                 // instances on the block schedule
+  const int *inst;           // their indices, largest first
+  int *ticket;               // zeroed before the launch
+  const int *seg_off;        // cells of instance g: [seg_off[g], seg_off[g + 1])
+  const int *inst_line_off;  // lines of instance g: [inst_line_off[g], inst_line_off[g + 1])
+  const int *line_off, *line_cells;
+  const T *la, *lcp, *linv;
+  const int *rowptr, *colidx;
+  const T *A;
+  T *b, *r, *r0, *p, *v, *s, *t, *ph, *sh, *y;
+  const int *newt_active;
+  int *lin_its;
+  double tol2;
+  int max_it;
+};
+
+// (a, b) and, with c, (c, d) over cells [i0, i1): chunk_dot_kernel's
+// accumulation and tree per chunk, chunk_sum_kernel's in-order sum; every
+// thread returns the result
+template <class TA, class TB>
+__device__ __forceinline__ void block_dot(int i0, int i1, const TA *a, const TB *b, const TA *c, const TB *d,
+                                          double *red, double *out1, double *out2) {
+  const int tid = threadIdx.x;
+  double tot = 0.0, tot2 = 0.0;
+  for (int k0 = i0; k0 < i1; k0 += kChunk) {
+    const int k1 = min(k0 + kChunk, i1);
+    double acc = 0.0, acc2 = 0.0;
+    for (int i = k0 + tid; i < k1; i += kBlockThreads) {
+      acc = op_dot(acc, a[i], b[i]);
+      if (c) acc2 = op_dot(acc2, c[i], d[i]);
+    }
+    red[tid] = acc;
+    red[kBlockThreads + tid] = acc2;
+    __syncthreads();
+    for (int w = kBlockThreads / 2; w > 0; w >>= 1) {
+      if (tid < w) {
+        red[tid] += red[tid + w];
+        red[kBlockThreads + tid] += red[kBlockThreads + tid + w];
+      }
+      __syncthreads();
+    }
+    tot += red[0];
+    tot2 += red[kBlockThreads];
+    __syncthreads();  // every thread has read the chunk's sums
+  }
+  *out1 = tot;
+  if (out2) *out2 = tot2;
+}
+
+// y = A x over rows [c0, c1): spmv_kernel's lane split and shuffle order
+template <class T, int TPR>
+__device__ __forceinline__ void block_spmv(int c0, int c1, const int *rowptr, const int *colidx, const T *A,
+                                           const T *x, T *y) {
+  const int nrow = c1 - c0;
+  for (int base = 0; base < nrow * TPR; base += kBlockThreads) {
+    const int gt = base + (int)threadIdx.x, rl = gt / TPR, lane = gt % TPR, row = c0 + rl;
+    T acc = 0;
+    if (rl < nrow)
+      for (int k = rowptr[row] + lane; k < rowptr[row + 1]; k += TPR) acc = e_fma(A[k], x[colidx[k]], acc);
+#pragma unroll
+    for (int o = TPR / 2; o > 0; o >>= 1) acc = e_add(acc, __shfl_down_sync(0xffffffffu, acc, o, TPR));
+    if (rl < nrow && lane == 0) y[row] = acc;
+  }
+}
+
+template <class T, int TPR>
+__global__ void __launch_bounds__(kBlockThreads) bicgstab_block_kernel(BlockSolve<T> B) {
+  __shared__ double red[2 * kBlockThreads];
+  __shared__ int cur;
+  const int tid = threadIdx.x;
+  for (;;) {
+    if (tid == 0) cur = atomicAdd(B.ticket, 1);
+    __syncthreads();
+    const int k = cur;
+    __syncthreads();  // every thread has read the ticket before the next one is drawn
+    if (k >= B.ninst) return;
+    const int g = B.inst[k];
+    const int c0 = B.seg_off[g], c1 = B.seg_off[g + 1];
+    const int l0 = B.inst_line_off[g], l1 = B.inst_line_off[g + 1];
+    int its = 0;
+    double bnorm2 = 0.0;
+    if (B.newt_active[g]) block_dot<T, T>(c0, c1, B.b, B.b, nullptr, nullptr, red, &bnorm2, nullptr);
+    if (bnorm2 > 0.0) {
+      double rho = 1.0, alpha = 1.0, omega = 1.0;
+      for (int it = 0; it < B.max_it; it++) {
+        double rn;
+        block_dot<T, T>(c0, c1, B.r0, B.r, nullptr, nullptr, red, &rn, nullptr);
+        if (rn == 0.0) break;
+        const double beta = (rn / rho) * (alpha / omega);
+        rho = rn;
+        {
+          const T tb = (T)beta, to = (T)omega;
+          for (int i = c0 + tid; i < c1; i += kBlockThreads) B.p[i] = op_p(B.r[i], B.p[i], B.v[i], tb, to);
+        }
+        __syncthreads();
+        for (int l = l0 + tid; l < l1; l += kBlockThreads)
+          line_solve_one(l, B.line_off, B.line_cells, B.la, B.lcp, B.linv, B.p, B.ph);
+        __syncthreads();
+        block_spmv<T, TPR>(c0, c1, B.rowptr, B.colidx, B.A, B.ph, B.v);
+        __syncthreads();
+        double dv;
+        block_dot<T, T>(c0, c1, B.r0, B.v, nullptr, nullptr, red, &dv, nullptr);
+        if (dv == 0.0) break;
+        alpha = rho / dv;
+        {
+          const T ta = (T)alpha;
+          for (int i = c0 + tid; i < c1; i += kBlockThreads) B.s[i] = e_fma(-ta, B.v[i], B.r[i]);
+        }
+        __syncthreads();
+        double ss;
+        block_dot<T, T>(c0, c1, B.s, B.s, nullptr, nullptr, red, &ss, nullptr);
+        const bool half = ss <= B.tol2 * bnorm2;
+        if (half) {
+          const T ta = (T)alpha;
+          for (int i = c0 + tid; i < c1; i += kBlockThreads) B.y[i] = op_y(B.y[i], B.ph[i], ta);
+          __syncthreads();
+          its++;
+          break;
+        }
+        for (int l = l0 + tid; l < l1; l += kBlockThreads)
+          line_solve_one(l, B.line_off, B.line_cells, B.la, B.lcp, B.linv, B.s, B.sh);
+        __syncthreads();
+        block_spmv<T, TPR>(c0, c1, B.rowptr, B.colidx, B.A, B.sh, B.t);
+        __syncthreads();
+        double tt, ts;
+        block_dot<T, T>(c0, c1, B.t, B.t, B.t, B.s, red, &tt, &ts);
+        omega = tt > 0.0 ? ts / tt : 0.0;
+        {
+          const T ta = (T)alpha, to = (T)omega;
+          for (int i = c0 + tid; i < c1; i += kBlockThreads) {
+            B.y[i] = op_y2(B.y[i], B.ph[i], B.sh[i], ta, to);
+            B.r[i] = e_fma(-to, B.t[i], B.s[i]);
+          }
+        }
+        __syncthreads();
+        double rr;
+        block_dot<T, T>(c0, c1, B.r, B.r, nullptr, nullptr, red, &rr, nullptr);
+        its++;
+        if (rr <= B.tol2 * bnorm2 || omega == 0.0) break;
+      }
+    }
+    if (tid == 0) B.lin_its[g] = its;
+    __syncthreads();
+  }
 }
 
 // trial point of the line search: x = xb - lam_s y for the instances on
@@ -645,18 +857,19 @@ void bicgstab_iteration(SolverState *s, Krylov &k, double tol2, Emit &e) {
   e(scal_check_kernel, sb, 128, 0, ns, act, s->lin_its, sc, tol2);
 }
 
+// (one allocation for the Jacobian copy and every vector; ordered on the
+// solve's stream, which uses them next)
 template <class T>
-int krylov_alloc(SolverState *s, Krylov &k) {
+int krylov_alloc(SolverState *s, Krylov &k, cudaStream_t st) {
   if (k.ready) return 0;
-  int ierr;
-  T *p;
-  if ((ierr = salloc(s, &p, s->nnz))) return ierr;
-  k.Jv = p;
-  void **vecs[] = {&k.b, &k.r, &k.r0, &k.p, &k.v, &k.s, &k.t, &k.ph, &k.sh, &k.y, &k.la, &k.lcp, &k.linv};
-  for (void **vp : vecs) {
-    if ((ierr = salloc(s, &p, s->n))) return ierr;
-    *vp = p;
-  }
+  Arena ar;
+  T **vecs[] = {(T **)&k.b, (T **)&k.r,  (T **)&k.r0, (T **)&k.p,  (T **)&k.v,   (T **)&k.s,   (T **)&k.t,
+                (T **)&k.ph, (T **)&k.sh, (T **)&k.y, (T **)&k.la, (T **)&k.lcp, (T **)&k.linv};
+  ar.work((T **)&k.Jv, (size_t)s->nnz);
+  for (T **vp : vecs) ar.work(vp, (size_t)s->n);
+  int ierr = ar.commit(st);
+  if (ierr) return ierr;
+  s->allocs.push_back(ar.base);
   k.ready = true;
   return 0;
 }
@@ -806,11 +1019,185 @@ int cluster_setup(SolverState *s, Krylov &k, double tau, cudaStream_t st) {
   return 0;
 }
 
+// Instances on the block schedule for a split at `thr` cells (-1: none,
+// LLONG_MAX: all): the list (largest first) and the per-instance mask.
+int set_block_split(SolverState *s, long long thr, cudaStream_t st) {
+  if (s->mask_for == thr) return 0;
+  std::vector<int> mask(s->nseg, 0), list;
+  for (int g : s->h_order) {
+    const long long nc = s->h_seg_off[g + 1] - s->h_seg_off[g];
+    if (thr >= 0 && nc <= thr) {
+      mask[g] = 1;
+      list.push_back(g);
+    }
+  }
+  s->n_block = (int)list.size();
+  s->n_tile = s->nseg - s->n_block;
+  SCUDA(cudaMemcpyAsync(s->block_mask, mask.data(), sizeof(int) * s->nseg, cudaMemcpyHostToDevice, st));
+  if (!list.empty())
+    SCUDA(cudaMemcpyAsync(s->block_inst, list.data(), sizeof(int) * list.size(), cudaMemcpyHostToDevice, st));
+  SCUDA(cudaStreamSynchronize(st));  // the host vectors are read
+  s->mask_for = thr;
+  return 0;
+}
+
+template <class T, int TPR>
+int launch_block(SolverState *s, Krylov &k, const TDyNewtonOptions &o, double tol2, cudaStream_t st) {
+  BlockSolve<T> B;
+  B.ninst = s->n_block;
+  B.inst = s->block_inst;
+  B.ticket = s->ticket;
+  B.seg_off = s->seg_off;
+  B.inst_line_off = s->inst_line_off;
+  B.line_off = s->line_off;
+  B.line_cells = s->line_cells;
+  B.la = (const T *)k.la;
+  B.lcp = (const T *)k.lcp;
+  B.linv = (const T *)k.linv;
+  B.rowptr = s->rowptr;
+  B.colidx = s->colidx;
+  B.A = (const T *)k.Jv;
+  B.b = (T *)k.b;
+  B.r = (T *)k.r;
+  B.r0 = (T *)k.r0;
+  B.p = (T *)k.p;
+  B.v = (T *)k.v;
+  B.s = (T *)k.s;
+  B.t = (T *)k.t;
+  B.ph = (T *)k.ph;
+  B.sh = (T *)k.sh;
+  B.y = (T *)k.y;
+  B.newt_active = s->newt_active;
+  B.lin_its = s->lin_its;
+  B.tol2 = tol2;
+  B.max_it = o.linear_max_it;
+  int dev = 0, nsm = 0, per_sm = 0;
+  SCUDA(cudaGetDevice(&dev));
+  SCUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  SCUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bicgstab_block_kernel<T, TPR>, kBlockThreads, 0));
+  const int grid = std::max(1, std::min(s->n_block, nsm * std::max(per_sm, 1)));
+  SCUDA(cudaMemsetAsync(s->ticket, 0, sizeof(int), st));
+  bicgstab_block_kernel<T, TPR><<<grid, kBlockThreads, 0, st>>>(B);
+  SCUDA(cudaGetLastError());
+  return 0;
+}
+
+// One linear solve with instances of at most `thr` cells on the block
+// schedule and the others on the tile schedule; its = inner iterations.
+template <class T>
+int solve_scheduled(SolverState *s, Krylov &k, const TDyNewtonOptions &o, double tol2, long long thr,
+                    cudaStream_t st, std::vector<int> &its) {
+  int ierr;
+  const int n = s->n, ns = s->nseg;
+  if ((ierr = set_block_split(s, thr, st))) return ierr;
+  init_kernel<T><<<nblk(n, 256), 256, 0, st>>>(n, s->cell_seg, s->newt_active, s->F, (T *)k.b, (T *)k.r, (T *)k.r0,
+                                               (T *)k.p, (T *)k.v, (T *)k.y);
+  {
+    Emit em(st);
+    dot<T>(s, (T *)k.b, (T *)k.b, nullptr, nullptr, S_BNORM2, 0, em);
+  }
+  SCUDA(cudaMemsetAsync(s->lin_its, 0, sizeof(int) * ns, st));
+  init_scalars_kernel<<<nblk(ns, 128), 128, 0, st>>>(ns, s->newt_active, s->block_mask, s->lin_active, s->lin_its,
+                                                     s->scal);
+  SCUDA(cudaGetLastError());
+  if (s->n_block > 0) {
+    switch (k.tpr) {
+      case 1:
+        ierr = launch_block<T, 1>(s, k, o, tol2, st);
+        break;
+      case 4:
+        ierr = launch_block<T, 4>(s, k, o, tol2, st);
+        break;
+      default:
+        ierr = launch_block<T, 8>(s, k, o, tol2, st);
+        break;
+    }
+    if (ierr) return ierr;
+  }
+  if (s->n_tile > 0) {
+    std::vector<int> act(ns);
+    const int check_every = 8;
+    for (int it = 0; it < o.linear_max_it; it += check_every) {
+      for (int j = 0; j < check_every && it + j < o.linear_max_it; j++) SCUDA(cudaGraphLaunch(k.graph, st));
+      SCUDA(cudaMemcpyAsync(act.data(), s->lin_active, sizeof(int) * ns, cudaMemcpyDeviceToHost, st));
+      SCUDA(cudaStreamSynchronize(st));
+      bool any = false;
+      for (int a : act) any |= (a != 0);
+      if (!any) break;
+    }
+  }
+  its.resize(ns);
+  SCUDA(cudaMemcpyAsync(its.data(), s->lin_its, sizeof(int) * ns, cudaMemcpyDeviceToHost, st));
+  SCUDA(cudaStreamSynchronize(st));
+  return 0;
+}
+
+// Schedule autotuner.  The first line-preconditioned solve of a size class
+// (arithmetic, number of instances, largest instance) times the candidate
+// splits on the solve at hand: all instances on the tile schedule, all on the
+// block schedule, and splits at 4096, 16384 and 65536 cells where they
+// separate the instances; the fastest split is kept for the class for the
+// rest of the process.  The schedules give the same bits, so the choice
+// changes only the time.
+std::mutex g_sched_mutex;
+std::vector<std::pair<long long, long long>> g_sched;  // (class key, split)
+
+template <class T>
+int tune_schedule(SolverState *s, Krylov &k, const TDyNewtonOptions &o, double tol2, cudaStream_t st,
+                  long long *thr) {
+  long long maxc = 0;
+  for (int g = 0; g < s->nseg; g++) maxc = std::max<long long>(maxc, s->h_seg_off[g + 1] - s->h_seg_off[g]);
+  int lg = 0;
+  while ((1LL << lg) < maxc) lg++;
+  const int cls = s->nseg == 1 ? 0 : (s->nseg < 64 ? 1 : 2);
+  const long long key = ((long long)sizeof(T) << 16) | ((long long)cls << 8) | lg;
+  if (s->block_max_cells != -2) {  // this handle's choice
+    *thr = s->block_max_cells;
+    return 0;
+  }
+  {
+    std::lock_guard<std::mutex> lk(g_sched_mutex);
+    for (auto &e : g_sched)
+      if (e.first == key) {
+        s->block_max_cells = *thr = e.second;
+        return 0;
+      }
+  }
+  std::vector<long long> cand = {-1, LLONG_MAX};
+  for (long long c : {4096LL, 16384LL, 65536LL}) {
+    int below = 0;
+    for (int g = 0; g < s->nseg; g++) below += (s->h_seg_off[g + 1] - s->h_seg_off[g]) <= c;
+    if (below > 0 && below < s->nseg) cand.push_back(c);
+  }
+  std::vector<int> its;
+  s->tune_ms.clear();
+  double best = 1e300;
+  long long best_thr = -1;
+  for (long long c : cand) {
+    int ierr;
+    if ((ierr = solve_scheduled<T>(s, k, o, tol2, c, st, its))) return ierr;  // warm-up
+    const auto t0 = std::chrono::steady_clock::now();
+    if ((ierr = solve_scheduled<T>(s, k, o, tol2, c, st, its))) return ierr;
+    const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    s->tune_ms.push_back(ms);
+    if (ms < best) {
+      best = ms;
+      best_thr = c;
+    }
+  }
+  {
+    std::lock_guard<std::mutex> lk(g_sched_mutex);
+    g_sched.emplace_back(key, best_thr);
+  }
+  s->block_max_cells = *thr = best_thr;
+  return 0;
+}
+
 template <class T>
 int linear_solve(SolverState *s, Krylov &k, const TDyNewtonOptions &o, cudaStream_t st, long long *lin_total,
                  std::vector<int> &inst_lin_its) {
   int ierr;
-  if ((ierr = krylov_alloc<T>(s, k))) return ierr;
+  if ((ierr = krylov_alloc<T>(s, k, st))) return ierr;
   if ((ierr = autotune_spmv<T>(s, k, st))) return ierr;  // uses b and v as scratch before they are set
   const int n = s->n, ns = s->nseg;
   cast_kernel<T><<<nblk(s->nnz, 256), 256, 0, st>>>(s->nnz, s->J, (T *)k.Jv);
@@ -819,15 +1206,6 @@ int linear_solve(SolverState *s, Krylov &k, const TDyNewtonOptions &o, cudaStrea
   if (s->precond_used == TDY_PRECOND_LINES)
     line_factor_kernel<T><<<nblk(s->nlines, 128), 128, 0, st>>>(s->nlines, s->line_off, s->pos_d, s->pos_lo,
                                                                  s->pos_hi, s->J, (T *)k.la, (T *)k.lcp, (T *)k.linv);
-  init_kernel<T><<<nblk(n, 256), 256, 0, st>>>(n, s->cell_seg, s->newt_active, s->F, (T *)k.b, (T *)k.r, (T *)k.r0,
-                                               (T *)k.p, (T *)k.v, (T *)k.y);
-  {
-    Emit em(st);
-    dot<T>(s, (T *)k.b, (T *)k.b, nullptr, nullptr, S_BNORM2, 0, em);
-  }
-  SCUDA(cudaMemsetAsync(s->lin_its, 0, sizeof(int) * ns, st));
-  init_scalars_kernel<<<nblk(ns, 128), 128, 0, st>>>(ns, s->newt_active, s->lin_active, s->lin_its, s->scal);
-  SCUDA(cudaGetLastError());
   const double tol2 = o.linear_rtol * o.linear_rtol;
   // The graph of one iteration is built with the explicit graph API, not by
   // stream capture: a capture is invalidated by device-wide operations that
@@ -853,18 +1231,19 @@ int linear_solve(SolverState *s, Krylov &k, const TDyNewtonOptions &o, cudaStrea
     k.graph_precond = s->precond_used;
     s->linear_rtol = o.linear_rtol;
   }
-  std::vector<int> act(ns), its(ns);
-  const int check_every = 8;
-  for (int it = 0; it < o.linear_max_it; it += check_every) {
-    for (int j = 0; j < check_every && it + j < o.linear_max_it; j++) SCUDA(cudaGraphLaunch(k.graph, st));
-    SCUDA(cudaMemcpyAsync(act.data(), s->lin_active, sizeof(int) * ns, cudaMemcpyDeviceToHost, st));
-    SCUDA(cudaStreamSynchronize(st));
-    bool any = false;
-    for (int a : act) any |= (a != 0);
-    if (!any) break;
+  std::vector<int> its(ns);
+  // the schedule split: chosen by timing on the first solve of this size
+  // class (process-wide), or given by the options; clusters: tile only
+  long long thr = -1;
+  if (s->precond_used == TDY_PRECOND_LINES) {
+    if (o.schedule == TDY_SCHEDULE_TILE)
+      thr = -1;
+    else if (o.schedule == TDY_SCHEDULE_BLOCK)
+      thr = LLONG_MAX;
+    else if ((ierr = tune_schedule<T>(s, k, o, tol2, st, &thr)))
+      return ierr;
   }
-  SCUDA(cudaMemcpyAsync(its.data(), s->lin_its, sizeof(int) * ns, cudaMemcpyDeviceToHost, st));
-  SCUDA(cudaStreamSynchronize(st));
+  if ((ierr = solve_scheduled<T>(s, k, o, tol2, thr, st, its))) return ierr;
   for (int v : its) *lin_total += v;
   inst_lin_its = its;
   return 0;
@@ -887,8 +1266,10 @@ int solver_init(_p_TDy *t) {
     return (q != e && *q == j) ? (int)(q - su.colidx.data()) : -1;
   };
   int c0 = 0;
+  std::vector<int> inst_line_off(1, 0);
   for (const ExtrudedInput &blk : t->mesh_blocks) {
     const int nc2 = blk.nc2, nl = blk.nlayers;
+    inst_line_off.push_back(inst_line_off.back() + nc2);
     for (int c2 = 0; c2 < nc2; c2++) {
       for (int k = 0; k < nl; k++) {
         const int i = c0 + k * nc2 + c2;
@@ -914,35 +1295,48 @@ int solver_init(_p_TDy *t) {
   }
   s->nchunks = (int)chunk_off.size() - 1;
   s->h_seg_off = seg_off;
+  s->h_inst_line_off = inst_line_off;
+  s->h_order.resize(s->nseg);
+  for (int g = 0; g < s->nseg; g++) s->h_order[g] = g;
+  std::stable_sort(s->h_order.begin(), s->h_order.end(),
+                   [&](int x, int y) { return seg_off[x + 1] - seg_off[x] > seg_off[y + 1] - seg_off[y]; });
   int ierr;
-  if ((ierr = sup(s, &s->rowptr, su.rowptr))) return ierr;
-  if ((ierr = sup(s, &s->colidx, su.colidx))) return ierr;
-  if ((ierr = sup(s, &s->seg_off, seg_off))) return ierr;
-  if ((ierr = sup(s, &s->chunk_off, chunk_off))) return ierr;
-  if ((ierr = sup(s, &s->seg_chunk, seg_chunk))) return ierr;
-  if ((ierr = salloc(s, &s->part, s->nchunks))) return ierr;
-  if ((ierr = salloc(s, &s->part2, s->nchunks))) return ierr;
-  if ((ierr = sup(s, &s->cell_seg, cell_seg))) return ierr;
-  if ((ierr = sup(s, &s->line_off, line_off))) return ierr;
-  if ((ierr = sup(s, &s->line_cells, line_cells))) return ierr;
-  if ((ierr = sup(s, &s->pos_d, pd))) return ierr;
+  // every array in one allocation, uploaded with one copy
   std::vector<int> dp(s->n);
   for (int i = 0; i < s->n; i++) dp[i] = find(i, i);  // every row has its diagonal (checked above per line cell)
-  if ((ierr = sup(s, &s->dpos, dp))) return ierr;
-  if ((ierr = sup(s, &s->pos_lo, plo))) return ierr;
-  if ((ierr = sup(s, &s->pos_hi, phi))) return ierr;
-  if ((ierr = salloc(s, &s->x, s->n))) return ierr;
-  if ((ierr = salloc(s, &s->xb, s->n))) return ierr;
-  if ((ierr = salloc(s, &s->lam, s->nseg))) return ierr;
-  if ((ierr = salloc(s, &s->trial, s->nseg))) return ierr;
-  if ((ierr = salloc(s, &s->commit, s->nseg))) return ierr;
-  if ((ierr = salloc(s, &s->F, s->n))) return ierr;
-  if ((ierr = salloc(s, &s->J, s->nnz))) return ierr;
-  if ((ierr = salloc(s, &s->fn2, s->nseg))) return ierr;
-  if ((ierr = salloc(s, &s->scal, (size_t)S_NSCAL * s->nseg))) return ierr;
-  if ((ierr = salloc(s, &s->newt_active, s->nseg))) return ierr;
-  if ((ierr = salloc(s, &s->lin_active, s->nseg))) return ierr;
-  if ((ierr = salloc(s, &s->lin_its, s->nseg))) return ierr;
+  Arena ar;
+  ar.up(&s->rowptr, su.rowptr);
+  ar.up(&s->colidx, su.colidx);
+  ar.up(&s->seg_off, seg_off);
+  ar.up(&s->chunk_off, chunk_off);
+  ar.up(&s->seg_chunk, seg_chunk);
+  ar.work(&s->part, s->nchunks);
+  ar.work(&s->part2, s->nchunks);
+  ar.up(&s->cell_seg, cell_seg);
+  ar.up(&s->line_off, line_off);
+  ar.up(&s->line_cells, line_cells);
+  ar.up(&s->pos_d, pd);
+  ar.up(&s->dpos, dp);
+  ar.up(&s->pos_lo, plo);
+  ar.up(&s->pos_hi, phi);
+  ar.work(&s->x, s->n);
+  ar.work(&s->xb, s->n);
+  ar.work(&s->lam, s->nseg);
+  ar.work(&s->trial, s->nseg);
+  ar.work(&s->commit, s->nseg);
+  ar.work(&s->F, s->n);
+  ar.work(&s->J, s->nnz);
+  ar.work(&s->fn2, s->nseg);
+  ar.work(&s->scal, (size_t)S_NSCAL * s->nseg);
+  ar.work(&s->newt_active, s->nseg);
+  ar.work(&s->lin_active, s->nseg);
+  ar.work(&s->lin_its, s->nseg);
+  ar.up(&s->inst_line_off, inst_line_off);
+  ar.work(&s->block_inst, s->nseg);
+  ar.work(&s->block_mask, s->nseg);
+  ar.work(&s->ticket, 1);
+  if ((ierr = ar.commit(s->st))) return ierr;
+  s->allocs.push_back(ar.base);
   // the allocations and uploads complete before any other stream uses them
   // (and before the host vectors above go out of scope)
   SCUDA(cudaStreamSynchronize(s->st));
@@ -978,6 +1372,7 @@ int device_be_solve(_p_TDy *t, double dt, double *dU, const TDyNewtonOptions &o,
   std::vector<double> y2(ns, 0.0), x2(ns, 0.0);
   std::vector<int> lin_its(ns, 0);  // inner iterations of the last solve, per instance
   long long lin_total = 0;
+  int fell_back = 0;
   // F and J at x (= xb for every instance after each evaluation below), and
   // the squared per-instance residual norms into g2
   auto evaluate = [&]() -> int {
@@ -1011,8 +1406,14 @@ int device_be_solve(_p_TDy *t, double dt, double *dU, const TDyNewtonOptions &o,
     }
     if (!any) break;
     SCUDA(cudaMemcpyAsync(s->newt_active, act.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, st));
+    // FP32 inner solves for the first fp32_max_it Newton iterations, FP64 after
+    // (an instance still iterating then is one whose FP32 directions stall;
+    // the switch depends only on the iteration number, so an instance takes it
+    // at the same point alone and in a batch)
+    const bool fp32 = o.linear_fp32 && (o.fp32_max_it < 0 || it < o.fp32_max_it);
+    if (o.linear_fp32 && !fp32) fell_back = 1;
     const void *y;
-    if (o.linear_fp32) {
+    if (fp32) {
       ierr = linear_solve<float>(s, s->k32, o, st, &lin_total, lin_its);
       y = s->k32.y;
     } else {
@@ -1024,7 +1425,7 @@ int device_be_solve(_p_TDy *t, double dt, double *dU, const TDyNewtonOptions &o,
     // the step at maxstep and ends with convergence by the step test when the
     // full step fails and ||y|| < stol ||x||
     {
-      if (o.linear_fp32)
+      if (fp32)
         seg_dot<float, float>(s, (const float *)y, (const float *)y, nullptr, nullptr, s->fn2, nullptr, st);
       else
         seg_dot<double, double>(s, (const double *)y, (const double *)y, nullptr, nullptr, s->fn2, nullptr, st);
@@ -1047,7 +1448,7 @@ int device_be_solve(_p_TDy *t, double dt, double *dU, const TDyNewtonOptions &o,
     for (int ls = 0; ls <= max_backtracks; ls++) {
       SCUDA(cudaMemcpyAsync(s->trial, trial.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, st));
       SCUDA(cudaMemcpyAsync(s->lam, lam.data(), sizeof(double) * ns, cudaMemcpyHostToDevice, st));
-      if (o.linear_fp32)
+      if (fp32)
         trial_kernel<float><<<nblk(n, 256), 256, 0, st>>>(n, s->cell_seg, s->trial, s->lam, (const float *)y, s->xb,
                                                           s->x);
       else
@@ -1101,7 +1502,7 @@ int device_be_solve(_p_TDy *t, double dt, double *dU, const TDyNewtonOptions &o,
     // norm of the step before its lambda scaling), so a step cut short by the
     // line search does not count as convergence.
     if (o.stol > 0.0) {
-      if (o.linear_fp32)
+      if (fp32)
         seg_dot<float, float>(s, (const float *)y, (const float *)y, nullptr, nullptr, s->fn2, nullptr, st);
       else
         seg_dot<double, double>(s, (const double *)y, (const double *)y, nullptr, nullptr, s->fn2, nullptr, st);
@@ -1143,6 +1544,9 @@ int device_be_solve(_p_TDy *t, double dt, double *dU, const TDyNewtonOptions &o,
     stats->clusters = s->precond_used == TDY_PRECOND_CLUSTERS ? s->ncl : 0;
     stats->cluster_cells = s->precond_used == TDY_PRECOND_CLUSTERS ? s->ncl_cells : 0;
     stats->cluster_cells_diagonal = s->precond_used == TDY_PRECOND_CLUSTERS ? s->ncl_big_cells : 0;
+    stats->fp64_fallback = fell_back;
+    stats->block_instances = s->precond_used == TDY_PRECOND_LINES ? s->n_block : 0;
+    stats->block_max_cells = s->precond_used == TDY_PRECOND_LINES ? s->mask_for : -1;
   }
   return 0;
 }

@@ -173,3 +173,18 @@ def test_hydrostatic_state_has_no_internal_flux():
     o = Oracle(_host(t))
     R, mag = o.ts_ifunction(U0, np.zeros_like(U0), with_mag=True)
     assert np.all(np.abs(R) <= 1e-12 * np.maximum(mag, 1e-300) + 1e-30)
+
+
+def test_oracle_threaded_residual_matches_serial():
+    """The oracle's threaded residual (vertex colours on threads, used for the
+    per-step checks of long runs) equals the serial one to rounding."""
+    T.options_clear()
+    t, U0, top, src, info = W.infiltration_prisms(300, 6)
+    t.setup(host_only=True)
+    o = Oracle(t.setup_view())
+    rng = np.random.default_rng(3)
+    U = U0 + rng.normal(0.0, 3e3, U0.size)
+    o.snes_presolve(U + rng.normal(0.0, 50.0, U0.size), 600.0)
+    R, M = o.snes_function(U, with_mag=True)
+    Rp = o.snes_function_parallel(U, 4)
+    assert np.all(np.abs(Rp - R) <= 1e-13 * M)

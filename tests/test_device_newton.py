@@ -157,7 +157,7 @@ def test_cluster_preconditioner_on_prisms():
 
 
 def test_cluster_factors_are_an_exact_inverse():
-    """With every coupling strong (threshold 0) a 54-cell column is one
+    """With every coupling strong (threshold 1e-300) a 54-cell column is one
     cluster, so its LU is the whole Jacobian's and the preconditioned FP64
     system is the identity: BiCGStab ends after one iteration at every Newton
     iteration, and the step equals the line-preconditioned one."""
@@ -177,7 +177,7 @@ def test_cluster_factors_are_an_exact_inverse():
     Un = 101325.0 + 998.0 * 9.8068 * (0.5 - zc) + np.random.default_rng(4).normal(0, 300, t.ncells)
     d = torch.tensor(Un, dtype=torch.float64, device="cuda")
     st, its, rel = t.backward_euler_step_device(d, DT, rtol=RTOL, fp32=False, precond="clusters",
-                                                cluster_threshold=0.0)
+                                                cluster_threshold=1e-300)
     assert st["converged"] == 1, st
     assert st["precond_used"] == T.PRECOND_CLUSTERS and st["clusters"] == 1 and st["cluster_cells"] == 54, st
     assert st["cluster_cells_diagonal"] == 0
@@ -189,3 +189,28 @@ def test_cluster_factors_are_an_exact_inverse():
     U1, U2 = d.cpu().numpy(), d2.cpu().numpy()
     assert np.max(np.abs(U1 - U2) / np.abs(U2)) < 1e-9
     assert oracle_rel_residual(t, Un, U1) <= 1.01 * RTOL
+
+
+@pytest.mark.parametrize("fp32", [True, False])
+def test_tile_and_block_schedules_give_the_same_bits(fp32):
+    """The inner solve's tile schedule (batch-wide kernels, one iteration a
+    graph) and block schedule (one CTA per instance) perform the same
+    operations in the same order: every instance gets the same bits, the
+    same Newton and inner iteration counts, from either, and from the
+    autotuned split."""
+    import torch
+
+    T.options_clear()
+    tb, U0, info = batched_columns(24, seed_offset=5)
+    tb.setup()
+    out = {}
+    for sched in ("tile", "block", "auto"):
+        d = torch.tensor(U0, dtype=torch.float64, device="cuda")
+        st, its, rel = tb.backward_euler_step_device(d, DT, rtol=RTOL, fp32=fp32, schedule=sched)
+        out[sched] = (d.cpu().numpy(), its.copy(), st)
+    assert out["block"][2]["block_instances"] == 24 and out["tile"][2]["block_instances"] == 0
+    for sched in ("block", "auto"):
+        assert np.array_equal(out[sched][0], out["tile"][0]), sched
+        assert np.array_equal(out[sched][1], out["tile"][1]), sched
+        assert out[sched][2]["linear_iterations"] == out["tile"][2]["linear_iterations"], sched
+    assert out["tile"][2]["converged"] + out["tile"][2]["step_converged"] == 24

@@ -60,6 +60,8 @@ def test_snes_parity(name, arith):
     Jr, Jm = o.snes_jacobian(U, with_mag=True)
     assert_close(R, Rr, Rm, R_TOL, f"{name} SNES residual")
     assert_close(J, Jr, Jm, J_TOL, f"{name} SNES Jacobian")
+    # norm-wise at these perturbed, non-equilibrium states
+    assert np.linalg.norm(R - Rr) <= R_TOL * np.linalg.norm(Rr), f"{name}: ||dR||/||R|| above {R_TOL}"
     # separate entry points agree with the fused one bit for bit
     assert np.array_equal(t.snes_function(U), R)
     assert np.array_equal(t.snes_jacobian(U), J)

@@ -1,8 +1,11 @@
-"""Layer-slab partition and halo exchange (multi-rank plan of the F+J path),
-tested on the CPU: the partition arithmetic in one process, and a two-rank
-gloo run in which every rank evaluates its owned rows of R and J (oracle, host
-setup of its local slab) after one ghost exchange, and the owned rows match
-the whole-mesh evaluation.
+"""Layer-slab partition and halo exchange (multi-rank plan of the F+J path):
+the partition arithmetic in one process; a two-rank gloo run on the CPU in
+which every rank evaluates its owned rows of R and J (oracle, host setup of
+its local slab) after one ghost exchange, and the owned rows match the
+whole-mesh evaluation; and the same two-rank run with the CUDA evaluation
+(each rank sets up its slab on the device, the ghosts travel through host
+buffers over gloo), whose owned rows equal the whole-mesh GPU evaluation bit
+for bit.
 """
 import os
 import socket
@@ -37,9 +40,9 @@ def global_fields():
     return dict(xy=xy, quads=quads, z=z, K=K, poro=poro, alpha=alpha, m=m, U=U, Uprev=Uprev)
 
 
-def build(f, levels, cells):
-    """Host setup of the mesh made of the given vertex levels, with the
-    properties of the given global cells."""
+def build(f, levels, cells, device=False):
+    """Setup (host only, or host and device) of the mesh made of the given
+    vertex levels, with the properties of the given global cells."""
     T.options_clear()
     t = T.create_richards_mpfao()
     t.set_extruded_mesh(f["xy"], f["quads"], f["z"][levels])
@@ -52,7 +55,7 @@ def build(f, levels, cells):
     t.set_water_density_type(T.WATER_DENSITY_EXPONENTIAL)
     t.set_boundary_pressure_type_function(top_dirichlet_types(f["z"].max()))
     t.set_boundary_pressure_function(lambda x, y, zz: 101325.0)
-    t.setup(host_only=True)
+    t.setup(host_only=not device)
     return t
 
 
@@ -103,7 +106,14 @@ def test_ghosts_are_the_fvm_overlap():
         assert np.array_equal(np.setdiff1d(cols, owned), s.cells[~s.owned])
 
 
-def _rank_main(rank, world, port, out_dir):
+def evaluate_gpu(t, U, Uprev):
+    """The CUDA evaluation through the host-pointer C-ABI."""
+    t.set_dtime(DT)
+    t.presolve(Uprev)
+    return t.snes_function_jacobian(U)
+
+
+def _rank_main(rank, world, port, out_dir, device=False):
     import torch.distributed as dist
 
     os.environ["MASTER_ADDR"] = "127.0.0.1"
@@ -122,9 +132,10 @@ def _rank_main(rank, world, port, out_dir):
         s.exchange(U, dist)
         s.exchange(Up, dist)
         assert np.array_equal(U, f["U"][s.cells]) and np.array_equal(Up, f["Uprev"][s.cells])
-        t = build(f, s.levels(), s.cells)
-        R, J = evaluate(t, U, Up)
+        t = build(f, s.levels(), s.cells, device=device)
+        R, J = (evaluate_gpu if device else evaluate)(t, U, Up)
         rows, rp, cols, vals = s.global_rows(t.rowptr, t.colidx, J)
+        t.destroy()
         np.savez(os.path.join(out_dir, f"rank{rank}.npz"), rows=rows, R=R[s.owned_local], rp=rp, cols=cols,
                  vals=vals)
     finally:
@@ -137,15 +148,15 @@ def _free_port():
         return so.getsockname()[1]
 
 
-def test_two_rank_halo_exchange_matches_whole_mesh(tmp_path):
+def _check_two_ranks(tmp_path, device):
     import torch.multiprocessing as mp
 
     world = 2
-    mp.spawn(_rank_main, args=(world, _free_port(), str(tmp_path)), nprocs=world, join=True)
+    mp.spawn(_rank_main, args=(world, _free_port(), str(tmp_path), device), nprocs=world, join=True)
     f = global_fields()
     ncol = NX * NY
-    t = build(f, slice(0, NZ + 1), np.arange(ncol * NZ))
-    R, J = evaluate(t, f["U"], f["Uprev"])
+    t = build(f, slice(0, NZ + 1), np.arange(ncol * NZ), device=device)
+    R, J = (evaluate_gpu if device else evaluate)(t, f["U"], f["Uprev"])
     seen = np.zeros(t.ncells, bool)
     for r in range(world):
         d = np.load(tmp_path / f"rank{r}.npz")
@@ -159,3 +170,16 @@ def test_two_rank_halo_exchange_matches_whole_mesh(tmp_path):
             assert np.array_equal(d["cols"][a:b], t.colidx[t.rowptr[i]:t.rowptr[i + 1]])
             assert np.array_equal(d["vals"][a:b], J[t.rowptr[i]:t.rowptr[i + 1]])
     assert seen.all()
+    t.destroy()
+
+
+def test_two_rank_halo_exchange_matches_whole_mesh(tmp_path):
+    _check_two_ranks(tmp_path, device=False)
+
+
+@pytest.mark.gpu
+def test_two_rank_cuda_slabs_match_whole_mesh_gpu(tmp_path):
+    """Two ranks on the one GPU (separate processes and contexts; their
+    kernels never wait on each other): owned rows of the CUDA evaluation of
+    each slab equal the whole-mesh CUDA evaluation bit for bit."""
+    _check_two_ranks(tmp_path, device=True)
