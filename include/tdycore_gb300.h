@@ -268,6 +268,8 @@ typedef struct {
   long long block_max_cells;    /* last inner solve: the split (instances up to this many cells on the block
                                    schedule; -1 none) */
   int fp64_fallback;            /* 1 if Newton went past fp32_max_it and finished with FP64 inner solves */
+  int eval_schedule;            /* evaluation of every instance: 0 three-stage launches, 1 one CTA per
+                                   instance (timed on the handle's first evaluation; the same bits) */
 } TDyNewtonStats;
 TDyErrorCode TDyNewtonOptionsDefault(TDyNewtonOptions *o);
 TDyErrorCode TDyGetNumInstances(TDy tdy, int *n);
@@ -303,6 +305,16 @@ TDyErrorCode TDyMPFAOSNESFunctionJacobianDevice(TDy tdy, const double *dU, doubl
 TDyErrorCode TDyMPFAOIFunctionIJacobianDevice(TDy tdy, double t, const double *dU, const double *dU_t, double shift,
                                               double *dR, double *dJ, void *stream);
 TDyErrorCode TDyPreSolveSNESSolverDevice(TDy tdy, const double *dU_prev, void *stream);
+/* Extension for batched handles (TDySetExtrudedMeshes; no reference
+ * counterpart): the SNES residual and Jacobian of the listed instances only
+ * (host array of ninst instance indices), in one launch with one CTA per
+ * instance at a time; the other instances' rows of dR and dJ are left as they
+ * are.  Each listed instance gets the same bits as from
+ * TDyMPFAOSNESFunctionJacobianDevice.  For Newton loops in which only some
+ * instances still iterate.  TDY_ERR_SUP when the handle's rows are longer
+ * than 96 entries. */
+TDyErrorCode TDyMPFAOSNESFunctionJacobianDeviceInstances(TDy tdy, const double *dU, double *dR, double *dJ,
+                                                         int ninst, const int *instances, void *stream);
 /* Same result as TDyMPFAOSNESFunctionJacobianDevice, but the call allocates
  * no device memory at all: its partial-sum scratch is a fixed 64 MiB array
  * built into the library (8,388,608 doubles; every GPU that loads the library

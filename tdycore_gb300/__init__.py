@@ -80,7 +80,7 @@ class NewtonStats(ctypes.Structure):
                 ("ninstances", c_int), ("max_rel_residual", c_double), ("step_converged", c_int),
                 ("precond_used", c_int), ("clusters", c_int), ("cluster_cells", c_int),
                 ("cluster_cells_diagonal", c_int), ("block_instances", c_int), ("block_max_cells", c_longlong),
-                ("fp64_fallback", c_int)]
+                ("fp64_fallback", c_int), ("eval_schedule", c_int)]
 
 
 def _sig(name, *args):
@@ -162,6 +162,7 @@ _sig("TDyMPFAOIFunctionIJacobianDevice", c_void_p, c_double, c_void_p, c_void_p,
      c_void_p)
 _sig("TDyPreSolveSNESSolverDevice", c_void_p, c_void_p, c_void_p)
 _sig("TDyMPFAOSNESFunctionJacobianDeviceNoAlloc", c_void_p, c_void_p, c_void_p, c_void_p, c_void_p)
+_sig("TDyMPFAOSNESFunctionJacobianDeviceInstances", c_void_p, c_void_p, c_void_p, c_void_p, c_int, _ip, c_void_p)
 _sig("TDyGetLaunchesPerEvaluation", c_void_p, _ip)
 _sig("TDySynchronize", c_void_p)
 _sig("TDyUpdateState", c_void_p, _dp, c_int)
@@ -656,6 +657,15 @@ class TDy:
         check(lib.TDyMPFAOSNESFunctionJacobianDevice(self._h, self._ptr(dU), self._ptr(dR), self._ptr(dJ),
                                                      self._ptr(stream) if stream is not None else None),
               "TDyMPFAOSNESFunctionJacobianDevice")
+
+    def snes_function_jacobian_device_instances(self, dU, dR, dJ, instances, stream=None):
+        """SNES R and J of the listed instances of a batched handle only (one
+        CTA per instance); the other rows of dR and dJ are left as they are."""
+        lst = _i32(instances)
+        check(lib.TDyMPFAOSNESFunctionJacobianDeviceInstances(self._h, self._ptr(dU), self._ptr(dR), self._ptr(dJ),
+                                                              lst.size, lst.ctypes.data_as(_ip),
+                                                              self._ptr(stream) if stream is not None else None),
+              "TDyMPFAOSNESFunctionJacobianDeviceInstances")
 
     def ifunction_ijacobian_device(self, t, dU, dUt, shift, dR, dJ, stream=None):
         check(lib.TDyMPFAOIFunctionIJacobianDevice(self._h, t, self._ptr(dU), self._ptr(dUt), shift, self._ptr(dR),

@@ -868,6 +868,14 @@ TDyErrorCode TDyMPFAOGetSetupView(TDy tdy, struct TDyMPFAOSetupView *v) {
   // on the device: bring it into the host arrays the view points at, once.
   if (tdy->opt.setup_on_device && tdy->dev && !tdy->trans_on_host) {
     MPFAOSetup &su = tdy->setup;
+    if (!su.dev_gen_vertex.empty()) {  // the other vertices built on the device
+      std::vector<double> tr;
+      int ierr = device_download_trans(tdy, tr);
+      if (ierr) return ierr;
+      for (int vtx : su.dev_gen_vertex)
+        std::copy(tr.begin() + su.v_trans_off[vtx], tr.begin() + su.v_trans_off[vtx + 1],
+                  su.trans.begin() + su.v_trans_off[vtx]);
+    }
     std::vector<double> Tc;
     int ierr = device_download_tc(tdy, Tc);
     if (ierr) return ierr;
@@ -1109,6 +1117,17 @@ TDyErrorCode TDyMPFAOSNESFunctionJacobianDevice(TDy tdy, const double *dU, doubl
   TDY_CHECK_DEVICE(tdy);
   if (!dU || (!dR && !dJ)) return set_error(TDY_ERR_ARG_NULL, "null array");
   return device_eval(tdy, FORM_SNES, 0.0, dU, nullptr, 0.0, dR, dJ, stream);
+}
+TDyErrorCode TDyMPFAOSNESFunctionJacobianDeviceInstances(TDy tdy, const double *dU, double *dR, double *dJ,
+                                                         int ninst, const int *instances, void *stream) {
+  TDY_CHECK_HANDLE(tdy);
+  TDY_CHECK_DEVICE(tdy);
+  if (!dU || (!dR && !dJ) || (ninst > 0 && !instances)) return set_error(TDY_ERR_ARG_NULL, "null array");
+  const int nblk = (int)tdy->mesh_blocks.size();
+  for (int k = 0; k < ninst; k++)
+    if (instances[k] < 0 || instances[k] >= nblk)
+      return set_error(TDY_ERR_ARG_OUTOFRANGE, "instance %d out of range [0, %d)", instances[k], nblk);
+  return device_eval_instances(tdy, dU, dR, dJ, instances, ninst, stream);
 }
 TDyErrorCode TDyMPFAOIFunctionIJacobianDevice(TDy tdy, double t, const double *dU, const double *dU_t, double shift,
                                               double *dR, double *dJ, void *stream) {

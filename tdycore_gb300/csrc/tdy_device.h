@@ -28,6 +28,11 @@ int device_eval(_p_TDy *t, int form, double time, const double *dU, const double
 int device_eval_host(_p_TDy *t, int form, double time, const double *U, const double *Ut, double shift, double *R,
                      double *J);
 int device_launches_per_eval(_p_TDy *t);
+// SNES-form evaluation of the listed instances (blocks) in one launch, one CTA
+// per instance (the same bits as device_eval); the others keep their R and J.
+int device_eval_instances(_p_TDy *t, const double *dU, double *dR, double *dJ, const int *list, int nlist,
+                          void *stream);
+bool device_inst_ok(_p_TDy *t);
 int device_synchronize(_p_TDy *t);
 int device_update_state_host(_p_TDy *t, const double *U);
 int device_get_diagnostic(_p_TDy *t, int which, double *out);
@@ -49,5 +54,10 @@ void device_solver_destroy(_p_TDy *t);
 int device_num_instances(_p_TDy *t);
 // Trans of the canonical vertices into d_Tc (-tdy_mpfao_setup_on_device).
 int device_canon_trans(const _p_TDy *t, const int *d_cellc, const int *d_facec, double *d_Tc, void *stream);
+// Trans of the other vertices marked by the set-up (setup.dev_gen_vertex), in
+// place in the device Trans array (-tdy_mpfao_setup_on_device).
+int device_gen_trans(const _p_TDy *t, double *d_trans, void *stream);
+// copies the device's generic Trans array (setup.ntrans) to the host
+int device_download_trans(_p_TDy *t, std::vector<double> &trans);
 
 }  // namespace tdy

@@ -172,7 +172,21 @@ struct MPFAOSetup {
   std::vector<int> sc_vc;          // 8 * nSpad
   std::vector<int> gc_cells;       // the other cells
   int max_nint = 0, max_nrow = 0, max_ncol = 0, max_row_nnz = 0;
+  // -tdy_mpfao_setup_on_device: other vertices whose Trans the device builds
+  // (one warp each) and the largest of their systems
+  std::vector<int> dev_gen_vertex;
+  int dev_gen_max_cells = 0, dev_gen_max_faces = 0, dev_gen_max_unk = 0, dev_gen_max_col = 0;
 };
+
+// Device-built Trans of other vertices: the limits of one warp's system
+// (cells, faces, shared-memory bytes: per cell 12 doubles and 3 ints, per
+// face 3 ints, A nunk x nunk and B nunk x ncol doubles).
+constexpr int kDevGenMaxCells = 48;
+constexpr int kDevGenMaxFaces = 96;
+constexpr size_t kDevGenMaxSmem = 48 * 1024;
+inline size_t dev_gen_smem_bytes(int ncell, int nface, int nunk, int ncol) {
+  return 8 * ((size_t)12 * ncell + (size_t)nunk * nunk + (size_t)nunk * ncol) + 4 * ((size_t)3 * ncell + 3 * nface);
+}
 
 int mpfao_setup(const Options &opt, const Mesh &m, const Materials &mat, const Boundary &bnd, MPFAOSetup &s);
 // Octant of each local cell and canonical row of each vertex row of a vertex

@@ -105,6 +105,14 @@ struct DevArgs {
   double *R, *J;
 };
 
+// The entities of one instance (block of a batched handle): cells [c0, c1),
+// boundary faces [b0, b1), canonical vertices [vc0, vc1), other vertices
+// gen_vertex[g0, g1), structured cells sc_cells[s0, s1), other cells
+// gc_cells[gc0, gc1).
+struct InstRange {
+  int c0, c1, b0, b1, vc0, vc1, g0, g1, s0, s1, gc0, gc1;
+};
+
 // timer groups: the state kernel, the vertex kernels, the cell kernels
 static const char *const kKernelNames[3] = {"state_kernel", "vertex_kernel", "cell_kernel"};
 
@@ -140,6 +148,15 @@ struct DeviceState {
   // recorded after its last enqueue: TDyDestroy waits for them before the
   // stream-ordered frees (which do not synchronise the device)
   std::vector<std::pair<cudaStream_t, cudaEvent_t>> user_streams;
+  // instance schedule (handles whose blocks are laid out contiguously):
+  // per-instance ranges, the list of a call, its ticket; smem bytes per CTA
+  InstRange *inst_rng = nullptr;
+  int *inst_list = nullptr, *inst_ticket = nullptr;
+  std::vector<InstRange> h_inst_rng;
+  std::vector<long long> h_inst_cells;
+  std::vector<int> h_list;
+  size_t inst_smem = 0;
+  bool inst_ok = false;
   // recorded after every allocation-free evaluation (created at set-up, so
   // that call creates nothing); such calls never overlap, so the last one
   // covers them all
@@ -279,10 +296,8 @@ __device__ __forceinline__ void viscosity(int type, double *vis, double *dvis) {
 // while the unsaturated cells, which cost ~50x more and cluster in space
 // (and therefore in cell numbering), spread over every SM instead of forming
 // a tail of a few slow blocks.
-__global__ void __launch_bounds__(256) state_kernel(DevArgs a, int nchunks, int chunk_mul) {
-  const int gw = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-  if (gw >= nchunks) return;
-  const int i = (int)(((long long)gw * chunk_mul) % nchunks) * 32 + (threadIdx.x & 31);
+// entity i: cell i < nc, else boundary face i - nc
+__device__ __forceinline__ void state_entity(const DevArgs &a, int i) {
   if (i < a.nc) {
     const double U = a.U[i];
     const double Pc = a.Pref - U;
@@ -368,6 +383,12 @@ __global__ void __launch_bounds__(256) state_kernel(DevArgs a, int nchunks, int 
     a.dlam[i] = 0.0;
     a.seep[i] = (a.bnd_type[b] == SEEPAGE_BC && p <= a.Pref) ? 1 : 0;
   }
+}
+
+__global__ void __launch_bounds__(256) state_kernel(DevArgs a, int nchunks, int chunk_mul) {
+  const int gw = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  if (gw >= nchunks) return;
+  state_entity(a, (int)(((long long)gw * chunk_mul) % nchunks) * 32 + (threadIdx.x & 31));
 }
 
 // Accumulation at the previous solution (TDyMPFAOSNESPreSolve,
@@ -465,12 +486,11 @@ __host__ __device__ constexpr int canon_row(int c, int k) {
 }
 __host__ __device__ constexpr bool canon_is_up(int c, int k) { return ((c >> k) & 1) == 0; }
 
+// canonical vertex vc; tid: its slot of the block's shared rows
 template <bool CONST_RHO, bool FFJ>
-__device__ __forceinline__ void canon_vertex(const DevArgs &a, int block) {
+__device__ __forceinline__ void canon_vertex_at(const DevArgs &a, int vc, int tid) {
   extern __shared__ double sh[];  // [36][blockDim]: w, E_up, E_dn per row
-  const int tid = threadIdx.x, bs = blockDim.x;
-  const int vc = a.vc0 + block * bs + tid;
-  if (vc >= a.vc1) return;
+  const int bs = blockDim.x;
   const long long P = a.nCpad;
   double p[8], hr[8], lam[8], dlam[8], hdr[8];
 #pragma unroll
@@ -626,9 +646,8 @@ __device__ __forceinline__ void canon_vertex(const DevArgs &a, int block) {
 //
 // (a) one thread per vertex, for meshes that are mostly canonical hexahedra
 // (their other vertices are few and small, and share the canonical launch)
-__device__ __forceinline__ void generic_vertex_thread(const DevArgs &a, int block) {
-  const int g = block * blockDim.x + threadIdx.x;
-  if (g >= a.ngen) return;
+// other vertex gen_vertex[g], one thread
+__device__ __forceinline__ void generic_vertex_one(const DevArgs &a, int g) {
   const int v = a.gen_vertex[g];
   const int nint = a.v_nint[v];
   const int r0 = a.v_row_off[v], nrow = a.v_row_off[v + 1] - r0;
@@ -803,10 +822,13 @@ __device__ __forceinline__ void generic_vertex_warp(const DevArgs &a, int block)
 // latency-bound gathers).
 template <bool CONST_RHO, bool FFJ>
 __global__ void __launch_bounds__(128) vertex_kernel(DevArgs a, int gen_blocks) {
-  if ((int)blockIdx.x >= gen_blocks)
-    canon_vertex<CONST_RHO, FFJ>(a, blockIdx.x - gen_blocks);
-  else
-    generic_vertex_thread(a, blockIdx.x);
+  if ((int)blockIdx.x >= gen_blocks) {
+    const int vc = a.vc0 + ((int)blockIdx.x - gen_blocks) * blockDim.x + threadIdx.x;
+    if (vc < a.vc1) canon_vertex_at<CONST_RHO, FFJ>(a, vc, threadIdx.x);
+  } else {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g < a.ngen) generic_vertex_one(a, g);
+  }
 }
 
 __global__ void __launch_bounds__(128) generic_vertex_kernel(DevArgs a) { generic_vertex_warp(a, blockIdx.x); }
@@ -820,12 +842,13 @@ __global__ void __launch_bounds__(128) generic_vertex_kernel(DevArgs a) { generi
 // with coalesced stores.  Both sum the vertices in the cell's corner order, so
 // a cell gets the same bits on either path.
 
-__device__ __forceinline__ void struct_cell(const DevArgs &a, int block) {
+// structured cell sc_cells[sidx]; the 32 lanes of a warp call it together
+// with consecutive sidx (those at or past s_end do nothing)
+__device__ __forceinline__ void struct_cell_at(const DevArgs &a, int sidx, int s_end) {
   extern __shared__ double rowbuf[];
-  const int sidx = block * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (sidx - lane >= a.nS) return;  // whole warp out of range
-  const bool active = sidx < a.nS;
+  if (sidx - lane >= s_end) return;  // whole warp out of range
+  const bool active = sidx < s_end;
   const int i = active ? a.sc_cells[sidx] : 0;
   const long long P = a.nCpad, Q = a.nSpad;
   const double *S = a.scratch;
@@ -882,13 +905,13 @@ __device__ __forceinline__ void struct_cell(const DevArgs &a, int block) {
 }
 
 // Other cells, thread form (meshes with structured cells).
-__device__ __forceinline__ void generic_cell_thread(const DevArgs &a, int block) {
+// other cell gc_cells[gidx], one thread
+__device__ __forceinline__ void generic_cell_at(const DevArgs &a, int gidx, int g_end) {
   extern __shared__ double rowbuf[];  // [warps][32 * max_row_nnz]
-  const int gidx = block * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int g0 = gidx - lane;
-  if (g0 >= a.ngc) return;  // whole warp out of range
-  const bool active = gidx < a.ngc;
+  if (g0 >= g_end) return;  // whole warp out of range
+  const bool active = gidx < g_end;
   const int i = active ? a.gc_cells[gidx] : -1;
   if (a.needR && active) {
     const int k0 = a.cv_off[i], k1 = a.cv_off[i + 1];
@@ -968,12 +991,47 @@ __device__ __forceinline__ void generic_cell_warp(const DevArgs &a, int block) {
 
 __global__ void __launch_bounds__(64) cell_kernel(DevArgs a, int struct_blocks) {
   if ((int)blockIdx.x < struct_blocks)
-    struct_cell(a, blockIdx.x);
+    struct_cell_at(a, blockIdx.x * blockDim.x + threadIdx.x, a.nS);
   else
-    generic_cell_thread(a, blockIdx.x - struct_blocks);
+    generic_cell_at(a, ((int)blockIdx.x - struct_blocks) * blockDim.x + threadIdx.x, a.ngc);
 }
 
 __global__ void __launch_bounds__(32 * kCellWarps) generic_cell_kernel(DevArgs a) { generic_cell_warp(a, blockIdx.x); }
+
+// ---------------------------------------------------------------------------
+// 5. instance schedule: one launch evaluates a list of instances (the blocks
+// of a batched handle), one CTA per instance at a time, taken from a ticket
+// counter; the CTA runs the instance's state, vertex and cell stages with
+// block barriers between them.  Every entity goes through the same device
+// function as in the three-stage launches (vertices and other cells in their
+// thread forms, which give the warp forms' bits), so an instance gets the same
+// bits from either schedule.  The instances not in the list keep their
+// previous R and J.
+constexpr int kInstThreads = 128;
+
+template <bool CONST_RHO, bool FFJ>
+__global__ void __launch_bounds__(kInstThreads) instance_eval_kernel(DevArgs a, const InstRange *rng, const int *list,
+                                                                     int nlist, int *ticket) {
+  __shared__ int cur;
+  const int tid = threadIdx.x, bs = blockDim.x;
+  for (;;) {
+    if (tid == 0) cur = atomicAdd(ticket, 1);
+    __syncthreads();
+    const int k = cur;
+    __syncthreads();  // every thread has read the ticket before the next one is drawn
+    if (k >= nlist) return;
+    const InstRange R = rng[list[k]];
+    for (int i = R.c0 + tid; i < R.c1; i += bs) state_entity(a, i);
+    for (int b = R.b0 + tid; b < R.b1; b += bs) state_entity(a, a.nc + b);
+    __syncthreads();
+    for (int vc = R.vc0 + tid; vc < R.vc1; vc += bs) canon_vertex_at<CONST_RHO, FFJ>(a, vc, tid);
+    for (int g = R.g0 + tid; g < R.g1; g += bs) generic_vertex_one(a, g);
+    __syncthreads();
+    for (int base = R.s0; base < R.s1; base += bs) struct_cell_at(a, base + tid, R.s1);
+    for (int base = R.gc0; base < R.gc1; base += bs) generic_cell_at(a, base + tid, R.gc1);
+    __syncthreads();
+  }
+}
 
 // ---------------------------------------------------------------------------
 // Host side
@@ -1089,6 +1147,65 @@ static void build_slabs(_p_TDy *t, DeviceState *d) {
     sl.j1 = s.rowptr[cut[k + 1]];
     d->slabs.push_back(sl);
   }
+}
+
+// Entity ranges of each block of the handle for the instance schedule; false
+// when some list does not run through the blocks in order (then the handle
+// evaluates with the three-stage launches only).
+static bool build_inst_ranges(const _p_TDy *t, std::vector<InstRange> &out, std::vector<long long> &cells) {
+  const Mesh &m = t->mesh;
+  const MPFAOSetup &s = t->setup;
+  const int nblk = (int)t->mesh_blocks.size();
+  std::vector<int> cb(nblk + 1, 0), vb(nblk + 1, 0);
+  for (int b = 0; b < nblk; b++) {
+    const ExtrudedInput &e = t->mesh_blocks[b];
+    cb[b + 1] = cb[b] + e.nc2 * e.nlayers;
+    vb[b + 1] = vb[b] + e.nv2 * (e.nlayers + 1);
+  }
+  if (cb[nblk] != m.nc || vb[nblk] != m.nv) return false;
+  auto block_of = [](const std::vector<int> &bounds, int x) {
+    return (int)(std::upper_bound(bounds.begin(), bounds.end(), x) - bounds.begin()) - 1;
+  };
+  // [first, last) position in `list` of the items of each block; false if unordered
+  auto ranges = [&](const std::vector<int> &list, const std::vector<int> &bounds, std::vector<int> &lo,
+                    std::vector<int> &hi, auto key) {
+    lo.assign(nblk, 0);
+    hi.assign(nblk, 0);
+    int prev = 0;
+    std::vector<int> first(nblk, -1), last(nblk, -1);
+    for (int i = 0; i < (int)list.size(); i++) {
+      const int b = block_of(bounds, key(list[i]));
+      if (b < prev) return false;
+      prev = b;
+      if (first[b] < 0) first[b] = i;
+      last[b] = i + 1;
+    }
+    int pos = 0;
+    for (int b = 0; b < nblk; b++) {
+      lo[b] = first[b] < 0 ? pos : first[b];
+      hi[b] = first[b] < 0 ? pos : last[b];
+      pos = hi[b];
+    }
+    return true;
+  };
+  auto ident = [](int x) { return x; };
+  std::vector<int> bcell(m.nb);
+  for (int b = 0; b < m.nb; b++) bcell[b] = m.face_cell1[m.bnd_face[b]];
+  std::vector<int> bidx(m.nb);
+  for (int b = 0; b < m.nb; b++) bidx[b] = b;
+  std::vector<int> blo, bhi, clo, chi, glo, ghi, slo, shi, gclo, gchi;
+  if (!ranges(bidx, cb, blo, bhi, [&](int b) { return bcell[b]; })) return false;
+  if (!ranges(s.canon_vertex, vb, clo, chi, ident)) return false;
+  if (!ranges(s.gen_vertex, vb, glo, ghi, ident)) return false;
+  if (!ranges(s.sc_cells, cb, slo, shi, ident)) return false;
+  if (!ranges(s.gc_cells, cb, gclo, gchi, ident)) return false;
+  out.resize(nblk);
+  cells.resize(nblk);
+  for (int b = 0; b < nblk; b++) {
+    out[b] = InstRange{cb[b], cb[b + 1], blo[b], bhi[b], clo[b], chi[b], glo[b], ghi[b], slo[b], shi[b], gclo[b], gchi[b]};
+    cells[b] = cb[b + 1] - cb[b];
+  }
+  return true;
 }
 
 static int noalloc_resolve(int dev);
@@ -1272,6 +1389,15 @@ int device_setup(_p_TDy *t) {
   ar.work(&d->dJ, d->nnz);
   ar.work(&d->diagS, m.nc);
   ar.work(&d->diagMass, m.nc);
+  // instance schedule: contiguous blocks and rows short enough for one CTA's
+  // shared rows (canonical vertices' 36 per thread, the cell rows)
+  d->inst_smem = (size_t)std::max(36, std::max(27, s.max_row_nnz)) * kInstThreads * sizeof(double);
+  d->inst_ok = s.max_row_nnz <= 96 && build_inst_ranges(t, d->h_inst_rng, d->h_inst_cells);
+  if (d->inst_ok) {
+    ar.up(&d->inst_rng, d->h_inst_rng);
+    ar.work(&d->inst_list, d->h_inst_rng.size());
+    ar.work(&d->inst_ticket, 1);
+  }
   if ((ierr = ar.commit(d->stream))) return ierr;
   d->allocs.push_back(ar.base);
   CUDA_TRY(cudaMemsetAsync(accum_prev, 0, sizeof(double) * m.nc, d->stream));
@@ -1279,6 +1405,7 @@ int device_setup(_p_TDy *t) {
   if (t->opt.setup_on_device &&
       (ierr = device_canon_trans(t, a.cellc, a.facec, const_cast<double *>(a.Tc), d->stream)))
     return ierr;
+  if (t->opt.setup_on_device && (ierr = device_gen_trans(t, const_cast<double *>(a.trans), d->stream))) return ierr;
   build_slabs(t, d);  // their copy stream and events are taken on first use
   if ((ierr = cell_smem_optin(d->device, cell_smem_bytes(a, cell_warp_form(a))))) return ierr;
   if ((ierr = noalloc_resolve(d->device))) return ierr;
@@ -1482,7 +1609,55 @@ int device_eval(_p_TDy *t, int form, double time, const double *dU, const double
   return 0;
 }
 
+// Instance-schedule evaluation (SNES form) of the listed instances (blocks);
+// the others keep their R and J.  TDY_ERR_SUP when the handle has no
+// instance ranges (blocks not contiguous, or rows too long).
+static size_t g_inst_smem_granted[kMaxDevices] = {};
+
+int device_eval_instances(_p_TDy *t, const double *dU, double *dR, double *dJ, const int *list, int nlist,
+                          void *stream) {
+  DeviceState *d = t->dev;
+  if (!d->inst_ok) return set_error(TDY_ERR_SUP, "instance schedule unavailable for this handle");
+  if (nlist <= 0) return 0;
+  cudaStream_t st = stream ? (cudaStream_t)stream : d->stream;
+  DevArgs a;
+  int ierr = eval_args(t, FORM_SNES, dU, nullptr, 0.0, dR, dJ, &a);
+  if (ierr) return ierr;
+  const bool cr = a.rho_type != WATER_DENSITY_EXPONENTIAL;
+  auto kern = cr ? (a.jac_ff ? instance_eval_kernel<true, true> : instance_eval_kernel<true, false>)
+                 : (a.jac_ff ? instance_eval_kernel<false, true> : instance_eval_kernel<false, false>);
+  if (d->inst_smem > 48 * 1024) {
+    std::lock_guard<std::mutex> lk(g_dev_mutex);
+    if (d->inst_smem > g_inst_smem_granted[d->device]) {
+      for (auto k : {instance_eval_kernel<true, true>, instance_eval_kernel<true, false>,
+                     instance_eval_kernel<false, true>, instance_eval_kernel<false, false>})
+        CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d->inst_smem));
+      g_inst_smem_granted[d->device] = d->inst_smem;
+    }
+  }
+  int nsm = 0, per_sm = 0;
+  CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, d->device));
+  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kInstThreads, d->inst_smem));
+  const int grid = std::max(1, std::min(nlist, nsm * std::max(per_sm, 1)));
+  d->h_list.assign(list, list + nlist);  // read by the copy before the caller's next synchronisation
+  CUDA_TRY(cudaMemcpyAsync(d->inst_list, d->h_list.data(), sizeof(int) * nlist, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemsetAsync(d->inst_ticket, 0, sizeof(int), st));
+  kern<<<grid, kInstThreads, d->inst_smem, st>>>(a, d->inst_rng, d->inst_list, nlist, d->inst_ticket);
+  CUDA_TRY(cudaGetLastError());
+  return note_stream(d, st);
+}
+
+bool device_inst_ok(_p_TDy *t) { return t->dev && t->dev->inst_ok; }
+
 void *device_default_stream(_p_TDy *t) { return t->dev ? (void *)t->dev->stream : nullptr; }
+
+int device_download_trans(_p_TDy *t, std::vector<double> &trans) {
+  const DeviceState *d = t->dev;
+  trans.resize(t->setup.trans.size());
+  if (!trans.empty())
+    CUDA_TRY(cudaMemcpy(trans.data(), d->a.trans, sizeof(double) * trans.size(), cudaMemcpyDeviceToHost));
+  return 0;
+}
 
 int device_download_tc(_p_TDy *t, std::vector<double> &Tc) {
   const DeviceState *d = t->dev;

@@ -376,6 +376,22 @@ int mpfao_setup(const Options &opt, const Mesh &m, const Materials &mat, const B
         continue;
       }
     }
+    // other vertices whose system fits one warp's shared memory: built on the
+    // device too (a placeholder here)
+    if (opt.setup_on_device && nint <= kDevGenMaxCells && nfv <= kDevGenMaxFaces &&
+        dev_gen_smem_bytes(nint, nfv, nunk, ncol) <= kDevGenMaxSmem) {
+      s.trans.insert(s.trans.end(), (size_t)nrow * ncol, 0.0);
+      s.dev_gen_vertex.push_back(v);
+      s.dev_gen_max_cells = std::max(s.dev_gen_max_cells, nint);
+      s.dev_gen_max_faces = std::max(s.dev_gen_max_faces, nfv);
+      s.dev_gen_max_unk = std::max(s.dev_gen_max_unk, nunk);
+      s.dev_gen_max_col = std::max(s.dev_gen_max_col, ncol);
+      for (int j = 0; j < nfv; j++) fpos[m.vert_faces[f0 + j]] = -1;
+      s.max_nint = std::max(s.max_nint, nint);
+      s.max_nrow = std::max(s.max_nrow, nrow);
+      s.max_ncol = std::max(s.max_ncol, ncol);
+      continue;
+    }
     // subcells and their flux coefficients
     // flux_{a,i} = sum_u cu[u] Pi_u + sum_k ck[k] P_D,k + ccell * P_a
     struct Flux {

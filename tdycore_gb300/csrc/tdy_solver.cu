@@ -140,6 +140,11 @@ struct SolverState {
   long long block_max_cells = -2, mask_for = -3;
   int n_block = 0, n_tile = 0;
   std::vector<double> tune_ms;  // measured candidates of the last tuning (ms per linear solve)
+  // evaluation of every instance: -1 not chosen, 0 three-stage launches,
+  // 1 instance schedule (timed on the first evaluation; the same bits)
+  int eval_mode = -1;
+  double eval_ms[2] = {0.0, 0.0};
+  std::vector<long long> h_inst_cells;
   // device memory: stream-ordered on the handle's stream (allocated there and
   // synchronised at init; freed there when the solver is destroyed, after
   // every solve has synchronised its stream)
@@ -1373,11 +1378,52 @@ int device_be_solve(_p_TDy *t, double dt, double *dU, const TDyNewtonOptions &o,
   std::vector<int> lin_its(ns, 0);  // inner iterations of the last solve, per instance
   long long lin_total = 0;
   int fell_back = 0;
+  std::vector<int> trial_list;
   // F and J at x (= xb for every instance after each evaluation below), and
   // the squared per-instance residual norms into g2
-  auto evaluate = [&]() -> int {
+  // `sub` (host list of instances, or null for all): only those instances'
+  // states changed since the last evaluation, the others keep F and J
+  std::vector<int> all_inst(ns);
+  for (int g = 0; g < ns; g++) all_inst[g] = g;
+  auto eval_all = [&]() -> int {
     int e;
-    if ((e = device_eval(t, FORM_SNES, 0.0, s->x, nullptr, 0.0, s->F, s->J, st))) return e;
+    if (s->eval_mode < 0 && device_inst_ok(t) && ns > 1) {
+      // time both schedules once on this evaluation (they give the same bits)
+      cudaEvent_t e0, e1;
+      SCUDA(cudaEventCreate(&e0));
+      SCUDA(cudaEventCreate(&e1));
+      for (int mode = 0; mode < 2; mode++) {
+        for (int rep = 0; rep < 2; rep++) {  // the first run warms up
+          SCUDA(cudaEventRecord(e0, st));
+          e = mode == 0 ? device_eval(t, FORM_SNES, 0.0, s->x, nullptr, 0.0, s->F, s->J, st)
+                        : device_eval_instances(t, s->x, s->F, s->J, all_inst.data(), ns, st);
+          if (e) return e;
+          SCUDA(cudaEventRecord(e1, st));
+          SCUDA(cudaEventSynchronize(e1));
+          float ms = 0.f;
+          SCUDA(cudaEventElapsedTime(&ms, e0, e1));
+          s->eval_ms[mode] = ms;
+        }
+      }
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      s->eval_mode = s->eval_ms[1] < s->eval_ms[0] ? 1 : 0;
+      return 0;
+    }
+    if (s->eval_mode < 0) s->eval_mode = 0;
+    return s->eval_mode == 1 ? device_eval_instances(t, s->x, s->F, s->J, all_inst.data(), ns, st)
+                             : device_eval(t, FORM_SNES, 0.0, s->x, nullptr, 0.0, s->F, s->J, st);
+  };
+  auto evaluate = [&](const std::vector<int> *sub = nullptr) -> int {
+    int e;
+    bool part = sub && (int)sub->size() < ns && device_inst_ok(t);
+    if (part)  // one CTA per instance: only for instances small enough for one SM
+      for (int g : *sub) part = part && s->h_seg_off[g + 1] - s->h_seg_off[g] <= 65536;
+    if (part)
+      e = device_eval_instances(t, s->x, s->F, s->J, sub->data(), (int)sub->size(), st);
+    else
+      e = eval_all();
+    if (e) return e;
     seg_dot<double, double>(s, s->F, s->F, nullptr, nullptr, s->fn2, nullptr, st);
     SCUDA(cudaGetLastError());
     SCUDA(cudaMemcpyAsync(g2.data(), s->fn2, sizeof(double) * ns, cudaMemcpyDeviceToHost, st));
@@ -1454,7 +1500,10 @@ int device_be_solve(_p_TDy *t, double dt, double *dU, const TDyNewtonOptions &o,
       else
         trial_kernel<double><<<nblk(n, 256), 256, 0, st>>>(n, s->cell_seg, s->trial, s->lam, (const double *)y, s->xb,
                                                            s->x);
-      if ((ierr = evaluate())) return ierr;
+      trial_list.clear();
+      for (int g = 0; g < ns; g++)
+        if (trial[g]) trial_list.push_back(g);
+      if ((ierr = evaluate(&trial_list))) return ierr;
       bool pending = false;
       for (int g = 0; g < ns; g++) {
         commit[g] = 0;
@@ -1545,6 +1594,7 @@ int device_be_solve(_p_TDy *t, double dt, double *dU, const TDyNewtonOptions &o,
     stats->cluster_cells = s->precond_used == TDY_PRECOND_CLUSTERS ? s->ncl_cells : 0;
     stats->cluster_cells_diagonal = s->precond_used == TDY_PRECOND_CLUSTERS ? s->ncl_big_cells : 0;
     stats->fp64_fallback = fell_back;
+    stats->eval_schedule = s->eval_mode;
     stats->block_instances = s->precond_used == TDY_PRECOND_LINES ? s->n_block : 0;
     stats->block_max_cells = s->precond_used == TDY_PRECOND_LINES ? s->mask_for : -1;
   }

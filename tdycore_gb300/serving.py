@@ -26,7 +26,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from . import NEUMANN_BC, WATER_DENSITY_CONSTANT, create_richards_mpfao, options_clear
+from . import NEUMANN_BC, WATER_DENSITY_CONSTANT, create_richards_mpfao, options_clear, options_insert
 from .workloads import GRAVITY, PREF, layered_z, structured_surface
 
 RHO = 998.0  # constant water density of the EOS used here (kg/m^3)
@@ -55,6 +55,7 @@ class Request:
     rel_residual: list = field(default_factory=list)
     converged_steps: int = 0
     step_test_steps: int = 0  # steps ended by the step test above the tolerance
+    setup_s: float = float("nan")  # building the request's handle (host mesh and layouts, Trans on the device)
     error: str | None = None
 
     @property
@@ -105,12 +106,16 @@ _opts_cleared = False
 
 
 def options_clear_once():
-    """Requests read no options; clear the database once per process so a
-    caller's leftovers do not leak into request handles."""
+    """Requests read one option: their interaction-region transmissibilities
+    are built on the device (-tdy_mpfao_setup_on_device), which shortens
+    admission.  The database is set once per process, so a caller's
+    leftovers do not leak into request handles (TDySetFromOptions only reads
+    it, from any thread)."""
     global _opts_cleared
     with _opts_lock:
         if not _opts_cleared:
             options_clear()
+            options_insert("-tdy_mpfao_setup_on_device")
             _opts_cleared = True
 
 
@@ -120,8 +125,10 @@ def run_request(req: Request, fp32: bool = True, dt: float = 3600.0, rtol: float
     import torch
 
     options_clear_once()
+    ts = time.perf_counter()
     t, U0, top = build(req)
     t.setup()
+    req.setup_s = time.perf_counter() - ts
     try:
         dU = torch.tensor(U0, dtype=torch.float64, device="cuda")
         torch.cuda.current_stream().synchronize()
@@ -233,8 +240,14 @@ def summary(reqs, wall_s: float):
     steps = sum(r.converged_steps for r in reqs)
     attempted = sum(len(r.rel_residual) for r in reqs)
     errs = [f"{r.rid}: {r.error}" for r in reqs if r.error is not None]
+    setup = np.array([r.setup_s for r in reqs if np.isfinite(r.setup_s)])
+    small = np.array([r.setup_s for r in reqs if np.isfinite(r.setup_s) and r.ncells < 100_000])
+    large = np.array([r.setup_s for r in reqs if np.isfinite(r.setup_s) and r.ncells >= 100_000])
     return {"requests": len(reqs), "errors": len(errs), "error_messages": errs[:3],
             "step_test_steps": sum(r.step_test_steps for r in reqs),
+            "setup_s_per_request": {"mean": float(setup.mean()) if setup.size else None,
+                                    "p50_small": float(np.percentile(small, 50)) if small.size else None,
+                                    "p50_large": float(np.percentile(large, 50)) if large.size else None},
             "p50_latency_s": float(np.percentile(lat, 50)) if lat.size else None,
             "p99_latency_s": float(np.percentile(lat, 99)) if lat.size else None,
             "solves_per_s": steps / wall_s, "converged_solves": steps, "solves_attempted": attempted,

@@ -1,9 +1,12 @@
 """A batch of independent instances as one handle (TDySetExtrudedMeshes):
 block-diagonal pattern, and each block's residual/Jacobian rows equal to
-those of the instance set up alone."""
+those of the instance set up alone; on the GPU, the one-CTA-per-instance
+evaluation gives the three-stage launches' bits."""
 import numpy as np
+import pytest
 
 import tdycore_gb300 as T
+from tdycore_gb300 import workloads as W
 from tdycore_gb300.workloads import layered_z, structured_surface
 from oracle import Oracle
 
@@ -67,3 +70,42 @@ def test_batch_blocks_match_instances():
         assert np.array_equal(o1.snes_function(U[c0:c1]), R[c0:c1])
         assert np.array_equal(o1.snes_jacobian(U[c0:c1]), J[tb.rowptr[c0]:tb.rowptr[c1]])
         assert np.array_equal(t1.colidx + c0, tb.colidx[tb.rowptr[c0]:tb.rowptr[c1]])
+
+
+@pytest.mark.gpu
+def test_instance_schedule_gives_the_three_stage_bits():
+    """One CTA per instance (TDyMPFAOSNESFunctionJacobianDeviceInstances)
+    gives every listed instance the bits of the three-stage launches, and
+    leaves the other instances' rows untouched."""
+    import torch
+
+    T.options_clear()
+    tb, U0, info = W.batched_columns(40, seed_offset=9)
+    tb.setup()
+    tb.set_dtime(3600.0)
+    dev = torch.device("cuda")
+    dU = torch.tensor(U0 + np.random.default_rng(1).normal(0.0, 500.0, U0.size), dtype=torch.float64, device=dev)
+    tb.presolve_device(torch.tensor(U0, dtype=torch.float64, device=dev))
+    R0 = torch.empty(tb.ncells, dtype=torch.float64, device=dev)
+    J0 = torch.empty(tb.nnz, dtype=torch.float64, device=dev)
+    tb.snes_function_jacobian_device(dU, R0, J0)
+    R1 = torch.full_like(R0, float("nan"))
+    J1 = torch.full_like(J0, float("nan"))
+    tb.snes_function_jacobian_device_instances(dU, R1, J1, list(range(40)))
+    torch.cuda.synchronize()
+    assert torch.equal(R0, R1) and torch.equal(J0, J1)
+    # a subset: listed rows recomputed bit for bit, the others left as they were
+    off = np.concatenate([[0], np.cumsum(info["instance_cells"])])
+    R2 = torch.full_like(R0, 7.0)
+    J2 = torch.full_like(J0, 7.0)
+    pick = [3, 17, 39]
+    tb.snes_function_jacobian_device_instances(dU, R2, J2, pick)
+    torch.cuda.synchronize()
+    R0h, R2h = R0.cpu().numpy(), R2.cpu().numpy()
+    J0h, J2h = J0.cpu().numpy(), J2.cpu().numpy()
+    mask = np.zeros(tb.ncells, bool)
+    for g in pick:
+        mask[off[g]:off[g + 1]] = True
+    assert np.array_equal(R2h[mask], R0h[mask]) and np.all(R2h[~mask] == 7.0)
+    rows = np.repeat(mask, np.diff(tb.rowptr))
+    assert np.array_equal(J2h[rows], J0h[rows]) and np.all(J2h[~rows] == 7.0)

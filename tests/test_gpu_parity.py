@@ -134,11 +134,14 @@ def test_double_float_jacobian_tracks_fp64(name):
 
 
 @pytest.mark.parametrize("name", ["spe10_small", "hydrostatic_box", "tpf_dirichlet", "mixed_curves", "seepage",
-                                  "neumann"])
+                                  "neumann", "wedge", "column", "single_cell"])
 def test_device_built_transmissibility(name):
-    """-tdy_mpfao_setup_on_device: the interior hexahedral vertices' Trans is
-    built by the device kernel, eliminating the interaction-region unknowns in
-    another order than the host.  R must meet the usual bar against the oracle
+    """-tdy_mpfao_setup_on_device: Trans is built by the device kernels (the
+    interior hexahedral vertices one thread each, eliminating the
+    interaction-region unknowns in another order than the host; the boundary,
+    prismatic and other vertices one warp each, with the host's system).
+    Wedge (prism), one-column and single-cell meshes are all boundary
+    vertices.  R must meet the usual bar against the oracle
     on the host-built setup.  For J the bar is taken relative to the larger of
     the entry's error scale and one FP64 unit (1e-16) of the largest scale in
     its row: entries that are structural zeros of Trans (orthogonal meshes)
@@ -166,7 +169,7 @@ def test_device_built_transmissibility(name):
     assert_close(J, Jr, np.maximum(Jm, 1e-16 * rowmax[row_of]), J_TOL, f"{name} SNES Jacobian, device-built Trans")
 
 
-@pytest.mark.parametrize("name", ["spe10_small", "tpf_dirichlet", "mixed_curves"])
+@pytest.mark.parametrize("name", ["spe10_small", "tpf_dirichlet", "mixed_curves", "wedge", "seepage", "column"])
 def test_device_built_trans_in_setup_view(name):
     """The setup view of a handle with device-built Trans holds the device
     values; they equal the host-built ones to rounding of the row scale."""
@@ -261,3 +264,44 @@ def test_pinned_and_pageable_host_buffers(name):
     t.snes_function_jacobian(U, Rp.numpy(), Jp.numpy())
     assert np.array_equal(Rp.numpy(), R1)
     assert np.array_equal(Jp.numpy(), J1)
+
+
+def test_device_built_transmissibility_prisms():
+    """Delaunay prisms with 3-D rotated K (every vertex non-hexahedral): the
+    device-built Trans equals the host's to rounding of each vertex block's
+    scale, and R and J meet the parity bars against the oracle on the
+    host-built setup."""
+    from tdycore_gb300 import workloads as W
+    import tdycore_gb300 as T_
+
+    def make(dev):
+        T_.options_clear()
+        if dev:
+            T_.options_insert("-tdy_mpfao_setup_on_device")
+        t, U0, top, src, info = W.infiltration_prisms(600, 5, rotation="full")
+        t.setup(host_only=not dev)
+        t.set_source_sink_values(src, cells=top)
+        return t, U0
+
+    t, U0 = make(True)
+    th, _ = make(False)
+    vd, vh = t.setup_view(), th.setup_view()
+    Td, Th = vd["trans"], vh["trans"]
+    for v in range(vh["nverts"]):
+        a, b = vh["v_trans_off"][v], vh["v_trans_off"][v + 1]
+        if a < b:
+            assert np.all(np.abs(Td[a:b] - Th[a:b]) <= 1e-13 * np.abs(Th[a:b]).max()), v
+    rng = np.random.default_rng(6)
+    U = U0 + rng.normal(0.0, 3e3, U0.size)
+    Uprev = U + rng.normal(0.0, 50.0, U0.size)
+    o = Oracle(vh)
+    t.set_dtime(DT)
+    t.presolve(Uprev)
+    o.snes_presolve(Uprev, DT)
+    R, J = t.snes_function_jacobian(U)
+    Rr, Rm = o.snes_function(U, with_mag=True)
+    Jr, Jm = o.snes_jacobian(U, with_mag=True)
+    assert_close(R, Rr, Rm, R_TOL, "prisms SNES residual, device-built Trans")
+    rowmax = np.maximum.reduceat(Jm, t.rowptr[:-1])
+    row_of = np.repeat(np.arange(t.ncells), np.diff(t.rowptr))
+    assert_close(J, Jr, np.maximum(Jm, 1e-16 * rowmax[row_of]), J_TOL, "prisms SNES Jacobian, device-built Trans")
