@@ -378,8 +378,12 @@ int mpfao_setup(const Options &opt, const Mesh &m, const Materials &mat, const B
     }
     // other vertices whose system fits one warp's shared memory: built on the
     // device too (a placeholder here)
+    // (the launch sizes every warp's shared memory by the largest cells,
+    // faces, unknowns and columns over these vertices: the bound holds for
+    // the running maxima)
     if (opt.setup_on_device && nint <= kDevGenMaxCells && nfv <= kDevGenMaxFaces &&
-        dev_gen_smem_bytes(nint, nfv, nunk, ncol) <= kDevGenMaxSmem) {
+        dev_gen_smem_bytes(std::max(nint, s.dev_gen_max_cells), std::max(nfv, s.dev_gen_max_faces),
+                           std::max(nunk, s.dev_gen_max_unk), std::max(ncol, s.dev_gen_max_col)) <= kDevGenMaxSmem) {
       s.trans.insert(s.trans.end(), (size_t)nrow * ncol, 0.0);
       s.dev_gen_vertex.push_back(v);
       s.dev_gen_max_cells = std::max(s.dev_gen_max_cells, nint);

@@ -679,7 +679,12 @@ int device_gen_trans(const _p_TDy *t, double *d_trans, void *stream) {
   if (ierr) return ierr;
   const size_t per_warp = 8 * ((size_t)12 * g.NI + (size_t)g.NU * g.NU + (size_t)g.NU * g.NC) +
                           8 * (((size_t)3 * g.NI + 3 * (size_t)g.NF + 1) / 2);
-  const size_t smem = per_warp * kGenTransWarps;
+  const size_t smem = per_warp * kGenTransWarps;  // at most 2 x 48 KB (the set-up bounds the maxima)
+  if (smem > 2 * kDevGenMaxSmem + 1024) {
+    cudaStreamSynchronize(cs);
+    dmem_free(ar.base, cs);
+    return set_error(TDY_ERR_LIB, "device Trans: %zu bytes of shared memory per block", smem);
+  }
   cudaError_t e = cudaMemsetAsync(status, 0, sizeof(int), cs);
   if (e == cudaSuccess && smem > 48 * 1024)
     e = cudaFuncSetAttribute(gen_trans_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
