@@ -574,6 +574,30 @@ def profile_prisms(ntri, evaluations, dt=3600.0):
     print(json.dumps({"profile_run": info["workload"], "ncells": nc, "nnz": nnz, "evaluations": evaluations}))
 
 
+def profile_batch(ninst, steps=2, dt=3600.0):
+    """Only the batched device Newton of ``ninst`` config-4 instances
+    (``steps`` backward-Euler steps from the same start, FP32 inner solves,
+    autotuned schedules), for profilers."""
+    import torch
+
+    import tdycore_gb300 as T
+    from tdycore_gb300.workloads import batched_columns
+
+    T.options_clear()
+    T.options_insert("-tdy_mpfao_setup_on_device")
+    tb, U0, info = batched_columns(ninst)
+    tb.setup()
+    out = []
+    for _ in range(steps):
+        d = torch.tensor(U0, dtype=torch.float64, device="cuda")
+        st, its, rel = tb.backward_euler_step_device(d, dt)
+        torch.cuda.synchronize()
+        out.append({k: st[k] for k in ("converged", "newton_iterations", "linear_iterations", "block_instances",
+                                        "eval_schedule")})
+    tb.destroy()
+    print(json.dumps({"profile_batch": info["workload"], "ncells": int(sum(info["instance_cells"])), "runs": out}))
+
+
 def serving_config5(nreq=160, rate=80.0, slots=32):
     """Config 5: Poisson arrivals of column/subdomain requests (5 % of them
     64 x 64 x 50 cells), 24 hourly backward-Euler steps each with top-flux
@@ -911,6 +935,8 @@ def main():
     ap.add_argument("--profile-prisms", type=int, default=0, metavar="NTRI",
                     help="only --steps device F+J evaluations of the prism workload with NTRI surface "
                          "triangles and 40 layers (for ncu)")
+    ap.add_argument("--profile-batch", type=int, default=0, metavar="NINST",
+                    help="only the batched device Newton of NINST config-4 instances (for ncu)")
     ap.add_argument("--profile", action="store_true",
                     help="time the device loop only (no timers, e2e, CPU or clock-fill loops), for ncu")
     args = ap.parse_args()
@@ -919,6 +945,8 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.profile_prisms > 0:
         profile_prisms(args.profile_prisms, args.steps)
+    elif args.profile_batch > 0:
+        profile_batch(args.profile_batch, max(1, min(args.steps, 4)))
     elif args.impl == "reference":
         run_reference(args, rank)
     else:
