@@ -602,20 +602,23 @@ def serving_config5(nreq=160, rate=80.0, slots=32):
     """Config 5: Poisson arrivals of column/subdomain requests (5 % of them
     64 x 64 x 50 cells), 24 hourly backward-Euler steps each with top-flux
     forcing, state resident on the device, admission by HBM footprint against
-    150 GB; continuous batching (``slots`` requests in flight, FP32 inner
-    solves) next to plain FP64 one-at-a-time serving of the same requests."""
+    150 GB; continuous batching (``slots`` workers, each serving a cohort of up
+    to 16 waiting requests as one batched handle, FP32 inner solves) next to
+    plain FP64 one-at-a-time serving of the same requests."""
     from tdycore_gb300 import serving as S
 
     out = {}
-    for name, kw in (("continuous_fp32", {"slots": slots, "fp32": True}),
-                     ("one_at_a_time_fp64", {"slots": 1, "fp32": False})):
+    for name, kw in (("continuous_fp32", {"slots": slots, "fp32": True, "cohort": 16}),
+                     ("one_at_a_time_fp64", {"slots": 1, "fp32": False, "cohort": 1})):
         reqs = S.make_requests(nreq, rate_per_s=rate, nsteps=24, large_fraction=0.05, seed=0)
         srv = S.Server(hbm_budget_bytes=150e9, **kw)
         t0 = time.perf_counter()
         done = srv.run(reqs)
         wall = time.perf_counter() - t0
         out[name] = S.summary(done, wall)
-        out[name]["peak_requests_in_flight"] = srv.peak_running
+        out[name]["peak_workers_in_flight"] = srv.peak_running
+        out[name]["cohorts"] = {"count": len(srv.cohorts), "mean_size": float(np.mean(srv.cohorts)),
+                                "max_size": int(max(srv.cohorts))}
         out[name]["peak_hbm_reserved_GB"] = srv.peak_in_use / 1e9
         log(f"config 5 {name}: {out[name]}")
     out["requests"] = nreq

@@ -273,6 +273,22 @@ typedef struct {
 } TDyNewtonStats;
 TDyErrorCode TDyNewtonOptionsDefault(TDyNewtonOptions *o);
 TDyErrorCode TDyGetNumInstances(TDy tdy, int *n);
+/* Extension for batched handles (no reference counterpart): which instances
+ * the next TDyBackwardEulerStepDevice calls advance (host array of
+ * ninstances flags; NULL: all).  An inactive instance keeps its state and
+ * costs no evaluation or inner solve; it is reported with 0 iterations and
+ * not counted as converged.  For a caller that retires some instances of a
+ * batch (a server whose request failed) and goes on with the others. */
+TDyErrorCode TDySetActiveInstances(TDy tdy, int ninstances, const int *active);
+/* Per-instance outcome of the last TDyBackwardEulerStepDevice call (host
+ * array of ninstances): TDY_INSTANCE_CONVERGED (FP64 residual met the
+ * tolerance), _STEP_TEST (ended by the step test above it), _NOT_CONVERGED,
+ * _INACTIVE (not advanced). */
+#define TDY_INSTANCE_NOT_CONVERGED 0
+#define TDY_INSTANCE_CONVERGED 1
+#define TDY_INSTANCE_STEP_TEST 2
+#define TDY_INSTANCE_INACTIVE 3
+TDyErrorCode TDyGetInstanceStatus(TDy tdy, int ninstances, int *status);
 /* inst_iterations and inst_rel_residual (host, ninstances entries) may be NULL. */
 TDyErrorCode TDyBackwardEulerStepDevice(TDy tdy, double dt, double *dU, const TDyNewtonOptions *opt,
                                         TDyNewtonStats *stats, int *inst_iterations, double *inst_rel_residual,

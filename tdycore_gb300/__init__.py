@@ -102,6 +102,9 @@ _sig("TDyOptionsHasName", c_char_p, _ip)
 _sig("TDyOutputRegression", c_void_p, _dp)
 _sig("TDyNewtonOptionsDefault", POINTER(NewtonOptions))
 _sig("TDyGetNumInstances", c_void_p, _ip)
+_sig("TDySetActiveInstances", c_void_p, c_int, _ip)
+_sig("TDyGetInstanceStatus", c_void_p, c_int, _ip)
+INSTANCE_NOT_CONVERGED, INSTANCE_CONVERGED, INSTANCE_STEP_TEST, INSTANCE_INACTIVE = 0, 1, 2, 3
 _sig("TDyBackwardEulerStepDevice", c_void_p, c_double, c_void_p, POINTER(NewtonOptions), POINTER(NewtonStats), _ip,
      _dp, c_void_p)
 _sig("TDyCreate", c_void_p, POINTER(c_void_p))
@@ -614,6 +617,21 @@ class TDy:
         n = c_int()
         check(lib.TDyGetNumInstances(self._h, byref(n)), "TDyGetNumInstances")
         return n.value
+
+    def set_active_instances(self, active=None):
+        """Instances the next device Newton steps advance (None: all)."""
+        if active is None:
+            check(lib.TDySetActiveInstances(self._h, 0, None), "TDySetActiveInstances")
+            return
+        a = _i32(active)
+        check(lib.TDySetActiveInstances(self._h, a.size, a.ctypes.data_as(_ip)), "TDySetActiveInstances")
+
+    def instance_status(self):
+        """Per-instance outcome of the last device Newton step (INSTANCE_*)."""
+        n = self.num_instances()
+        st = np.zeros(n, dtype=np.int32)
+        check(lib.TDyGetInstanceStatus(self._h, n, st.ctypes.data_as(_ip)), "TDyGetInstanceStatus")
+        return st
 
     def backward_euler_step_device(self, dU, dt, rtol=1e-8, atol=0.0, max_it=50, fp32=True, linear_rtol=1e-6,
                                    linear_max_it=400, stol=1e-8, stream=None, precond="lines",

@@ -1048,6 +1048,29 @@ TDyErrorCode TDyNewtonOptionsDefault(TDyNewtonOptions *o) {
   o->fp32_max_it = 8;
   return 0;
 }
+TDyErrorCode TDySetActiveInstances(TDy tdy, int ninstances, const int *active) {
+  TDY_CHECK_HANDLE(tdy);
+  if (!active) {
+    tdy->inst_active.clear();
+    return 0;
+  }
+  if (ninstances != (int)tdy->mesh_blocks.size())
+    return set_error(TDY_ERR_ARG_OUTOFRANGE, "TDySetActiveInstances: %d flags for %d instances", ninstances,
+                     (int)tdy->mesh_blocks.size());
+  tdy->inst_active.assign(active, active + ninstances);
+  return 0;
+}
+TDyErrorCode TDyGetInstanceStatus(TDy tdy, int ninstances, int *status) {
+  TDY_CHECK_HANDLE(tdy);
+  if (!status) return set_error(TDY_ERR_ARG_NULL, "TDyGetInstanceStatus: null");
+  if (ninstances != (int)tdy->mesh_blocks.size())
+    return set_error(TDY_ERR_ARG_OUTOFRANGE, "TDyGetInstanceStatus: %d entries for %d instances", ninstances,
+                     (int)tdy->mesh_blocks.size());
+  if ((int)tdy->inst_status.size() != ninstances)
+    return set_error(TDY_ERR_USER, "TDyGetInstanceStatus: no device Newton step yet");
+  std::copy(tdy->inst_status.begin(), tdy->inst_status.end(), status);
+  return 0;
+}
 TDyErrorCode TDyGetNumInstances(TDy tdy, int *n) {
   TDY_CHECK_HANDLE(tdy);
   if (!n) return set_error(TDY_ERR_ARG_NULL, "TDyGetNumInstances: null");

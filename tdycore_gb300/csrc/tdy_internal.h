@@ -251,6 +251,8 @@ struct _p_TDy {
   std::vector<double> U_prev;
   tdy::DeviceState *dev = nullptr;
   tdy::SolverState *solver = nullptr;  // device Newton solver, on first use
+  std::vector<int> inst_active;        // instances the device Newton advances (empty: all)
+  std::vector<int> inst_status;        // outcome per instance of the last device Newton step
   bool trans_on_host = false;          // device-built Trans copied into setup.trans
 };
 

@@ -1374,6 +1374,13 @@ int device_be_solve(_p_TDy *t, double dt, double *dU, const TDyNewtonOptions &o,
   SCUDA(cudaMemcpyAsync(s->xb, dU, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
   std::vector<double> f0(ns, 0.0), fn(ns, 0.0), g2(ns, 0.0), lam(ns, 1.0);
   std::vector<int> act(ns, 1), its(ns, 0), trial(ns, 0), commit(ns, 0), step_conv(ns, 0), failed(ns, 0);
+  // instances retired by the caller are not advanced (TDySetActiveInstances)
+  const bool masked = (int)t->inst_active.size() == ns;
+  std::vector<int> live;
+  for (int g = 0; g < ns; g++) {
+    if (masked && !t->inst_active[g]) act[g] = 0;
+    if (act[g]) live.push_back(g);
+  }
   std::vector<double> y2(ns, 0.0), x2(ns, 0.0);
   std::vector<int> lin_its(ns, 0);  // inner iterations of the last solve, per instance
   long long lin_total = 0;
@@ -1430,7 +1437,7 @@ int device_be_solve(_p_TDy *t, double dt, double *dU, const TDyNewtonOptions &o,
     SCUDA(cudaStreamSynchronize(st));
     return 0;
   };
-  if ((ierr = evaluate())) return ierr;
+  if ((ierr = evaluate(masked ? &live : nullptr))) return ierr;
   for (int g = 0; g < ns; g++) f0[g] = fn[g] = std::sqrt(g2[g]);
   const double alpha = 1e-4;  // sufficient-decrease constant of PETSc's backtracking line search
   constexpr double kMaxStep = 1e8;  // PETSc's default SNESLineSearch maxstep
@@ -1570,13 +1577,18 @@ int device_be_solve(_p_TDy *t, double dt, double *dU, const TDyNewtonOptions &o,
   SCUDA(cudaMemcpyAsync(dU, s->xb, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
   SCUDA(cudaStreamSynchronize(st));
   int conv = 0, conv_step = 0, maxit = 0;
+  t->inst_status.assign(ns, TDY_INSTANCE_NOT_CONVERGED);
   double worst = 0.0;
   for (int g = 0; g < ns; g++) {
-    const double rel = f0[g] > 0.0 ? fn[g] / f0[g] : 0.0;
-    const bool fin = !failed[g] && std::isfinite(fn[g]);
+    const bool retired = masked && !t->inst_active[g];
+    const double rel = (f0[g] > 0.0 && !retired) ? fn[g] / f0[g] : 0.0;
+    const bool fin = !retired && !failed[g] && std::isfinite(fn[g]);
     const bool ok = fin && (!(fn[g] > o.atol) || rel <= o.rtol);
     conv += ok ? 1 : 0;
     conv_step += (fin && !ok && step_conv[g]) ? 1 : 0;
+    t->inst_status[g] = retired ? TDY_INSTANCE_INACTIVE
+                                : ok ? TDY_INSTANCE_CONVERGED
+                                     : (fin && step_conv[g]) ? TDY_INSTANCE_STEP_TEST : TDY_INSTANCE_NOT_CONVERGED;
     worst = std::max(worst, rel);
     maxit = std::max(maxit, its[g]);
     if (inst_its) inst_its[g] = its[g];

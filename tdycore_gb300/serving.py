@@ -8,11 +8,16 @@ the whole request.
 
 Serving is continuous: a request that arrives while others are on the GPU is
 admitted as soon as a slot and enough of the HBM budget are free, and its
-steps overlap on the device with those of the requests already running (each
-request owns a handle, hence its own CUDA stream and device buffers, and is
-driven by a worker thread; the C-ABI calls release the interpreter lock).
-Requests never share device state, and every kernel is deterministic, so a
-request's result is the same alone and in any mix.
+steps overlap on the device with those of the requests already running.
+Requests are admitted in cohorts: when a slot frees up, the requests that
+have arrived and wait (up to ``cohort`` of them, consecutive in arrival
+order and of one size class) become one batched handle, each request an
+instance, driven by one worker thread (the C-ABI calls release the
+interpreter lock).  A cohort's Newton iterations evaluate and solve only its
+instances still iterating (one CTA per instance), and a request that fails
+a step is retired from its cohort.  An instance gets the same bits alone and
+in any batch (every schedule gives the same bits, reductions are chunked per
+instance), so a request's result is the same alone and in any mix.
 
 No reference counterpart: TDycore runs one problem per process through
 PETSc.
@@ -155,18 +160,130 @@ def run_request(req: Request, fp32: bool = True, dt: float = 3600.0, rtol: float
         t.destroy()
 
 
+LARGE_CELLS = 100_000  # requests of at least this many cells form cohorts of one
+
+
+def size_class(r: Request) -> int:
+    return 1 if r.ncells >= LARGE_CELLS else 0
+
+
+def build_cohort(reqs):
+    """One batched handle for ``reqs`` (each request's mesh a block, with the
+    properties, boundary conditions and initial state ``build`` gives it
+    alone); returns (handle, U0, top cells per request)."""
+    blocks, K, poro, m, alpha, sr, U0, tops = [], [], [], [], [], [], [], []
+    off = 0
+    for r in reqs:
+        xy, quads = structured_surface(r.nx, r.ny, r.cell * r.nx, r.cell * r.ny)
+        depth = r.dz * r.nz
+        blocks.append((xy, quads, layered_z(xy.shape[0], r.nz, depth)))
+        n = r.ncells
+        k = np.zeros((n, 9))
+        k[:, 0] = k[:, 4] = k[:, 8] = r.k
+        K.append(k)
+        poro.append(np.full(n, r.porosity))
+        m.append(np.full(n, r.m))
+        alpha.append(np.full(n, r.alpha))
+        sr.append(np.full(n, r.sr))
+        zc = (np.arange(r.nz) + 0.5) * r.dz
+        p = PREF + RHO * GRAVITY * (0.6 * depth - zc)
+        U0.append(np.repeat(p, r.nx * r.ny) + np.random.default_rng(1000 + r.rid).normal(0.0, 10.0, n))
+        tops.append(off + np.arange((r.nz - 1) * r.nx * r.ny, n, dtype=np.int32))
+        off += n
+    t = create_richards_mpfao()
+    t.set_extruded_meshes(blocks)
+    t.set_from_options()
+    t.set_permeability_values(np.concatenate(K))
+    t.set_porosity_values(np.concatenate(poro))
+    mm = np.concatenate(m)
+    t.set_vangenuchten_values(mm, np.concatenate(alpha))
+    t.set_mualem_values(mm)
+    t.set_residual_saturation_values(np.concatenate(sr))
+    t.set_water_density_type(WATER_DENSITY_CONSTANT)
+    t.set_boundary_pressure_type_function(lambda x, y, zz: np.full(np.shape(x), NEUMANN_BC))
+    return t, np.concatenate(U0), tops
+
+
+def run_cohort(reqs, fp32: bool = True, dt: float = 3600.0, rtol: float = 1e-8, finished=None):
+    """All steps of the requests of one cohort on the calling thread: one
+    batched handle, each request an instance; a request that does not
+    converge a step is retired (its error recorded) and the others go on.
+    ``finished(r)`` is called as each request completes."""
+    import torch
+
+    from . import INSTANCE_CONVERGED, INSTANCE_STEP_TEST
+
+    options_clear_once()
+    ts = time.perf_counter()
+    t, U0, tops = build_cohort(reqs)
+    t.setup()
+    setup_s = time.perf_counter() - ts
+    for r in reqs:
+        r.setup_s = setup_s
+    top_all = np.concatenate(tops)
+    area = np.concatenate([np.full(tp.size, r.cell * r.cell) for r, tp in zip(reqs, tops)])
+    try:
+        dU = torch.tensor(U0, dtype=torch.float64, device="cuda")
+        torch.cuda.current_stream().synchronize()
+        done = [False] * len(reqs)
+        for k in range(max(len(r.forcing) for r in reqs)):
+            active = np.array([not done[i] and k < len(r.forcing) for i, r in enumerate(reqs)], dtype=np.int32)
+            if not active.any():
+                break
+            q = np.concatenate([np.full(tp.size, r.forcing[k] if active[i] else 0.0)
+                                for i, (r, tp) in enumerate(zip(reqs, tops))])
+            t.set_source_sink_values(RHO * q * area, cells=top_all)
+            t.set_active_instances(active)
+            stats, its, rel = t.backward_euler_step_device(dU, dt, rtol=rtol, fp32=fp32)
+            status = t.instance_status()
+            for i, r in enumerate(reqs):
+                if not active[i]:
+                    continue
+                r.newton_its.append(int(its[i]))
+                r.rel_residual.append(float(rel[i]))
+                if status[i] == INSTANCE_CONVERGED:
+                    r.converged_steps += 1
+                elif status[i] == INSTANCE_STEP_TEST:
+                    r.step_test_steps += 1
+                else:
+                    r.error = f"step {k + 1} did not converge (relative residual {rel[i]:.1e})"
+                if r.error is not None or k + 1 == len(r.forcing):
+                    done[i] = True
+                    if r.error is None:
+                        c0, c1 = (int(tops[i][0]) - (r.nz - 1) * r.nx * r.ny, int(tops[i][-1]) + 1)
+                        r.U_final = dU[c0:c1].cpu().numpy()
+                    if finished:
+                        finished(r)
+        Uh = dU.cpu().numpy()
+        off = np.concatenate([[0], np.cumsum([r.ncells for r in reqs])])
+        for i, r in enumerate(reqs):
+            if r.U_final is None:
+                r.U_final = Uh[off[i]:off[i + 1]].copy()
+    finally:
+        t.destroy()
+
+
 class Server:
     """Admits requests in arrival order as slots and HBM budget allow and runs
-    them concurrently (``slots`` worker threads)."""
+    them concurrently (``slots`` worker threads), ``cohort`` requests of one
+    size class at most per worker (``cohort=1``: one handle per request)."""
 
     def __init__(self, slots: int = 32, hbm_budget_bytes: float = 150e9, fp32: bool = True, dt: float = 3600.0,
-                 runner=None, footprint=footprint_bytes, clock=time.perf_counter):
+                 runner=None, footprint=footprint_bytes, clock=time.perf_counter, cohort: int = 16):
         self.slots, self.budget, self.fp32, self.dt = slots, float(hbm_budget_bytes), fp32, dt
-        self.runner = runner or (lambda req: run_request(req, fp32=self.fp32, dt=self.dt))
+        self.cohort = max(1, cohort)
+        if runner is None:
+            if self.cohort == 1:
+                runner = lambda reqs, finished: run_request(reqs[0], fp32=self.fp32, dt=self.dt)  # noqa: E731
+            else:
+                runner = lambda reqs, finished: run_cohort(reqs, fp32=self.fp32, dt=self.dt,  # noqa: E731
+                                                           finished=finished)
+        self.runner = runner
         self.footprint = footprint
         self.clock = clock
         self.peak_in_use = 0.0
         self.peak_running = 0
+        self.cohorts = []  # sizes of the cohorts formed
 
     def run(self, requests):
         """Serves ``requests`` (their arrival_s relative to the start) and
@@ -179,38 +296,61 @@ class Server:
         in_use, running = [0.0], [0]
         start = self.clock()
 
-        def work(r):
+        def finished(r):
+            with lock:
+                if r.finished_s != r.finished_s:  # NaN: not yet finished
+                    r.finished_s = self.clock() - start
+
+        def work(group):
             try:
-                self.runner(r)
+                self.runner(group, finished)
             except Exception as e:  # reported per request
-                r.error = repr(e)
+                for r in group:
+                    if r.error is None:
+                        r.error = repr(e)
             finally:
                 with lock:
-                    r.finished_s = self.clock() - start
-                    in_use[0] -= self.footprint(r.ncells)
+                    for r in group:
+                        if r.finished_s != r.finished_s:
+                            r.finished_s = self.clock() - start
+                        in_use[0] -= self.footprint(r.ncells)
                     running[0] -= 1
                     lock.notify_all()
 
         i = 0
         with ThreadPoolExecutor(self.slots) as pool:
             while i < len(reqs):
-                r = reqs[i]
                 with lock:
                     now = self.clock() - start
-                    if r.arrival_s > now:
-                        lock.wait(timeout=r.arrival_s - now)
+                    if reqs[i].arrival_s > now:
+                        lock.wait(timeout=reqs[i].arrival_s - now)
                         continue
-                    need = self.footprint(r.ncells)
-                    if running[0] >= self.slots or in_use[0] + need > self.budget:
+                    if running[0] >= self.slots:
+                        lock.wait(timeout=0.05)
+                        continue
+                    # the arrived requests that wait, consecutive in arrival
+                    # order, one size class, within the budget
+                    cls, cap = size_class(reqs[i]), (1 if size_class(reqs[i]) else self.cohort)
+                    group, need = [], 0.0
+                    j = i
+                    while (j < len(reqs) and len(group) < cap and reqs[j].arrival_s <= now
+                           and size_class(reqs[j]) == cls
+                           and in_use[0] + need + self.footprint(reqs[j].ncells) <= self.budget):
+                        need += self.footprint(reqs[j].ncells)
+                        group.append(reqs[j])
+                        j += 1
+                    if not group:
                         lock.wait(timeout=0.05)
                         continue
                     in_use[0] += need
                     running[0] += 1
                     self.peak_in_use = max(self.peak_in_use, in_use[0])
                     self.peak_running = max(self.peak_running, running[0])
-                    r.admitted_s = now
-                pool.submit(work, r)
-                i += 1
+                    for r in group:
+                        r.admitted_s = now
+                    self.cohorts.append(len(group))
+                pool.submit(work, group)
+                i = j
         return reqs
 
 

@@ -26,7 +26,8 @@ def test_admission_respects_slots_budget_and_order():
     reqs = _requests(n, rng.integers(1, 10, n), rng.uniform(0.0, 0.004, n))
     live, peak, lock = [0], [0], threading.Lock()
 
-    def runner(r):
+    def runner(group, finished):
+        (r,) = group
         with lock:
             live[0] += 1
             peak[0] = max(peak[0], live[0])
@@ -35,7 +36,7 @@ def test_admission_respects_slots_budget_and_order():
             live[0] -= 1
 
     fp = lambda nc: 10 * nc  # noqa: E731  budget units per cell
-    srv = S.Server(slots=4, hbm_budget_bytes=100, runner=runner, footprint=fp)
+    srv = S.Server(slots=4, hbm_budget_bytes=100, runner=runner, footprint=fp, cohort=1)
     done = srv.run(reqs)
     assert all(r.error is None for r in done)
     assert peak[0] <= 4 and srv.peak_running <= 4
@@ -44,7 +45,38 @@ def test_admission_respects_slots_budget_and_order():
     assert admitted == sorted(admitted), "admission follows arrival order"
     assert all(r.admitted_s >= r.arrival_s - 1e-9 and r.finished_s > r.admitted_s for r in done)
     with pytest.raises(ValueError):
-        S.Server(slots=2, hbm_budget_bytes=5, runner=runner, footprint=fp).run(_requests(1, [1], [0.0]))
+        S.Server(slots=2, hbm_budget_bytes=5, runner=runner, footprint=fp, cohort=1).run(_requests(1, [1], [0.0]))
+
+
+def test_cohorts_are_consecutive_same_class_and_within_budget():
+    """Requests that have arrived and wait when a slot frees up form one
+    cohort: consecutive in arrival order, of one size class (large requests
+    alone), at most ``cohort`` of them, within the HBM budget."""
+    reqs = _requests(30, [5] * 30, [0.0] * 30)
+    for r in reqs[10:13]:
+        r.nx, r.ny, r.nz = 64, 64, 50  # large
+    seen, lock = [], threading.Lock()
+
+    def runner(group, finished):
+        with lock:
+            seen.append([r.rid for r in group])
+        for r in group:
+            finished(r)
+        time.sleep(0.02)
+
+    fp = lambda nc: nc  # noqa: E731
+    srv = S.Server(slots=1, hbm_budget_bytes=1e6, runner=runner, footprint=fp, cohort=4)
+    done = srv.run(reqs)
+    assert all(r.error is None and r.finished_s >= r.admitted_s for r in done)
+    flat = [rid for g in seen for rid in g]
+    assert flat == sorted(flat) == list(range(30)), "every request once, in arrival order"
+    for g in seen:
+        assert len(g) <= 4
+        cls = {S.size_class(reqs[rid]) for rid in g}
+        assert len(cls) == 1
+        if cls == {1}:
+            assert len(g) == 1
+    assert max(len(g) for g in seen) == 4 and srv.cohorts == [len(g) for g in seen]
 
 
 def test_request_generator_statistics():
@@ -80,8 +112,10 @@ def test_summary_counts_converged_solves_and_completed_requests():
 
 @pytest.mark.gpu
 def test_same_result_alone_and_in_the_mix():
+    """Requests served in cohorts (one batched handle each) give every request
+    the bits it gets alone."""
     reqs = S.make_requests(8, rate_per_s=400.0, nsteps=3, large_fraction=0.0, seed=5)
-    srv = S.Server(slots=4)
+    srv = S.Server(slots=4, cohort=4)
     mix = srv.run(reqs)
     assert all(r.error is None for r in mix), [r.error for r in mix]
     assert all(r.converged_steps + r.step_test_steps == 3 for r in mix)
@@ -99,7 +133,7 @@ def test_concurrent_requests_with_overlapping_setup_and_teardown():
     handles.  No request may fail for any reason but a step that does not
     converge, and a request's result is the same as when it runs alone."""
     reqs = S.make_requests(24, rate_per_s=5000.0, nsteps=2, large_fraction=0.0, seed=11)
-    srv = S.Server(slots=16)
+    srv = S.Server(slots=16, cohort=1)
     done = srv.run(reqs)
     assert srv.peak_running >= 16
     bad = [r.error for r in done if r.error is not None and "did not converge" not in r.error]
