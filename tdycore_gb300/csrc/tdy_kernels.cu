@@ -253,9 +253,12 @@ __device__ __forceinline__ void relperm(int type, const double *p, double Se, do
 
 // EOSComputeWaterDensity / EOSComputeWaterViscosity (tdyeos.c:5-136) at
 // T = Tref and zero salinity.
+// EOSComputeWaterDensity_Constant (tdyeos.c:5-14)
+constexpr double kRhoConst = 998.0;
+
 __device__ __forceinline__ void density(int type, double p, double *rho, double *drho, double *d2rho) {
   if (type == WATER_DENSITY_CONSTANT) {
-    *rho = 998.0;
+    *rho = kRhoConst;
     *drho = 0.0;
     *d2rho = 0.0;
   } else if (type == WATER_DENSITY_EXPONENTIAL) {
@@ -486,9 +489,30 @@ __host__ __device__ constexpr int canon_row(int c, int k) {
 }
 __host__ __device__ constexpr bool canon_is_up(int c, int k) { return ((c >> k) & 1) == 0; }
 
+// x < 0.0 by integer operations (the FP64 pipe is this kernel's bound):
+// the sign bit set, and neither a zero nor a NaN
+__device__ __forceinline__ bool dneg(double x) {
+  const long long b = __double_as_longlong(x), m = b & 0x7fffffffffffffffLL;
+  return b < 0 && m != 0 && m <= 0x7ff0000000000000LL;
+}
+
+// first canonical row that touches octant o
+__host__ __device__ constexpr int canon_first_row(int o) {
+  for (int r = 0; r < 12; r++)
+    if (canon_up(r) == o || canon_dn(r) == o) return r;
+  return -1;
+}
+
+// Density modes of the canonical vertex: RHO_CONST (constant density: the
+// face average 2 (rho/2) is the constant itself, rho/2 is not gathered),
+// RHO_NODERIV (density without a pressure derivative), RHO_EXP (exponential,
+// with its derivative).
+enum { RHO_CONST = 0, RHO_NODERIV = 1, RHO_EXP = 2 };
+
 // canonical vertex vc; tid: its slot of the block's shared rows
-template <bool CONST_RHO, bool FFJ>
+template <int RHO, bool FFJ>
 __device__ __forceinline__ void canon_vertex_at(const DevArgs &a, int vc, int tid) {
+  constexpr bool CONST_RHO = RHO != RHO_EXP;
   extern __shared__ double sh[];  // [36][blockDim]: w, E_up, E_dn per row
   const int bs = blockDim.x;
   const long long P = a.nCpad;
@@ -497,14 +521,12 @@ __device__ __forceinline__ void canon_vertex_at(const DevArgs &a, int vc, int ti
   for (int o = 0; o < 8; o++) {
     const int cell = a.cellc[o * P + vc];
     p[o] = a.P[cell];
-    hr[o] = a.hr[cell];
+    hr[o] = RHO == RHO_CONST ? 0.5 * kRhoConst : a.hr[cell];
     lam[o] = a.lam[cell];
     dlam[o] = a.dlam[cell];
     hdr[o] = CONST_RHO ? 0.0 : a.hdr[cell];
   }
   double Rv[8];
-#pragma unroll
-  for (int o = 0; o < 8; o++) Rv[o] = 0.0;
 #pragma unroll
   for (int r = 0; r < 12; r++) {
     const int u = canon_up(r), d = canon_dn(r);
@@ -514,14 +536,22 @@ __device__ __forceinline__ void canon_vertex_at(const DevArgs &a, int vc, int ti
 #pragma unroll
     for (int c = 1; c < 8; c++) TP = __fma_rn(T[c * P], p[c], TP);
     const double G = a.G[a.facec[r * P + vc]];
-    const double den = __dadd_rn(hr[u], hr[d]);
+    // (constant density: 499 + 499, exactly the constant)
+    const double den = RHO == RHO_CONST ? kRhoConst : __dadd_rn(hr[u], hr[d]);
     const double q = __fma_rn(den, G, TP);
-    const bool fdn = q < 0.0;
+    const bool fdn = dneg(q);
     const double lm = fdn ? lam[u] : lam[d];
     const double w = __dmul_rn(den, lm);
     const double flux = -__dmul_rn(w, q);
-    Rv[u] += flux;
-    Rv[d] -= flux;
+    // an octant's partial residual starts from its first row's flux
+    if (r == canon_first_row(u))
+      Rv[u] = flux;
+    else
+      Rv[u] += flux;
+    if (r == canon_first_row(d))
+      Rv[d] = -flux;
+    else
+      Rv[d] -= flux;
     if (a.needJ) {
       // derivative of the flux with respect to the up and down cell pressures
       // beyond w*T: d(rho_avg)/dP and d(kr/mu)/dP of the upwind cell
@@ -820,11 +850,11 @@ __device__ __forceinline__ void generic_vertex_warp(const DevArgs &a, int block)
 // they overlap the canonical ones; meshes without canonical vertices launch
 // the warp form on its own (a light kernel with high occupancy for its
 // latency-bound gathers).
-template <bool CONST_RHO, bool FFJ>
+template <int RHO, bool FFJ>
 __global__ void __launch_bounds__(128) vertex_kernel(DevArgs a, int gen_blocks) {
   if ((int)blockIdx.x >= gen_blocks) {
     const int vc = a.vc0 + ((int)blockIdx.x - gen_blocks) * blockDim.x + threadIdx.x;
-    if (vc < a.vc1) canon_vertex_at<CONST_RHO, FFJ>(a, vc, threadIdx.x);
+    if (vc < a.vc1) canon_vertex_at<RHO, FFJ>(a, vc, threadIdx.x);
   } else {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g < a.ngen) generic_vertex_one(a, g);
@@ -1009,7 +1039,7 @@ __global__ void __launch_bounds__(32 * kCellWarps) generic_cell_kernel(DevArgs a
 // previous R and J.
 constexpr int kInstThreads = 128;
 
-template <bool CONST_RHO, bool FFJ>
+template <int RHO, bool FFJ>
 __global__ void __launch_bounds__(kInstThreads) instance_eval_kernel(DevArgs a, const InstRange *rng, const int *list,
                                                                      int nlist, int *ticket) {
   __shared__ int cur;
@@ -1024,7 +1054,7 @@ __global__ void __launch_bounds__(kInstThreads) instance_eval_kernel(DevArgs a, 
     for (int i = R.c0 + tid; i < R.c1; i += bs) state_entity(a, i);
     for (int b = R.b0 + tid; b < R.b1; b += bs) state_entity(a, a.nc + b);
     __syncthreads();
-    for (int vc = R.vc0 + tid; vc < R.vc1; vc += bs) canon_vertex_at<CONST_RHO, FFJ>(a, vc, tid);
+    for (int vc = R.vc0 + tid; vc < R.vc1; vc += bs) canon_vertex_at<RHO, FFJ>(a, vc, tid);
     for (int g = R.g0 + tid; g < R.g1; g += bs) generic_vertex_one(a, g);
     __syncthreads();
     for (int base = R.s0; base < R.s1; base += bs) struct_cell_at(a, base + tid, R.s1);
@@ -1508,6 +1538,12 @@ static int launch_state(const DevArgs &a, cudaStream_t st) {
 // canonical): the warp form in its own launch, then the canonical ones; else
 // one launch with the thread form in the first blocks.  The choice is made
 // once per mesh, so a slab launches the same form as the whole evaluation.
+static int rho_mode(const DevArgs &a) {
+  return a.rho_type == WATER_DENSITY_CONSTANT ? RHO_CONST
+         : a.rho_type == WATER_DENSITY_EXPONENTIAL ? RHO_EXP
+                                                   : RHO_NODERIV;
+}
+
 static int launch_vertices(const DevArgs &a, bool gen_warp, cudaStream_t st) {
   if (gen_warp && a.ngen > 0) {
     const size_t gen_smem = (size_t)kGenWarps * a.gen_warp_doubles * sizeof(double);
@@ -1515,16 +1551,20 @@ static int launch_vertices(const DevArgs &a, bool gen_warp, cudaStream_t st) {
   }
   const size_t canon_smem = 36 * 128 * sizeof(double);
   const int cb = (int)nblocks(a.vc1 - a.vc0, 128), gb = gen_warp ? 0 : (int)nblocks(a.ngen, 128);
-  const bool cr = a.rho_type != WATER_DENSITY_EXPONENTIAL;
   if (cb + gb > 0) {
-    if (cr && a.jac_ff)
-      vertex_kernel<true, true><<<cb + gb, 128, canon_smem, st>>>(a, gb);
-    else if (cr)
-      vertex_kernel<true, false><<<cb + gb, 128, canon_smem, st>>>(a, gb);
+    const int rho = rho_mode(a);
+    if (rho == RHO_CONST && a.jac_ff)
+      vertex_kernel<RHO_CONST, true><<<cb + gb, 128, canon_smem, st>>>(a, gb);
+    else if (rho == RHO_CONST)
+      vertex_kernel<RHO_CONST, false><<<cb + gb, 128, canon_smem, st>>>(a, gb);
+    else if (rho == RHO_NODERIV && a.jac_ff)
+      vertex_kernel<RHO_NODERIV, true><<<cb + gb, 128, canon_smem, st>>>(a, gb);
+    else if (rho == RHO_NODERIV)
+      vertex_kernel<RHO_NODERIV, false><<<cb + gb, 128, canon_smem, st>>>(a, gb);
     else if (a.jac_ff)
-      vertex_kernel<false, true><<<cb + gb, 128, canon_smem, st>>>(a, gb);
+      vertex_kernel<RHO_EXP, true><<<cb + gb, 128, canon_smem, st>>>(a, gb);
     else
-      vertex_kernel<false, false><<<cb + gb, 128, canon_smem, st>>>(a, gb);
+      vertex_kernel<RHO_EXP, false><<<cb + gb, 128, canon_smem, st>>>(a, gb);
   }
   return 0;
 }
@@ -1623,14 +1663,15 @@ int device_eval_instances(_p_TDy *t, const double *dU, double *dR, double *dJ, c
   DevArgs a;
   int ierr = eval_args(t, FORM_SNES, dU, nullptr, 0.0, dR, dJ, &a);
   if (ierr) return ierr;
-  const bool cr = a.rho_type != WATER_DENSITY_EXPONENTIAL;
-  auto kern = cr ? (a.jac_ff ? instance_eval_kernel<true, true> : instance_eval_kernel<true, false>)
-                 : (a.jac_ff ? instance_eval_kernel<false, true> : instance_eval_kernel<false, false>);
+  using Kern = void (*)(DevArgs, const InstRange *, const int *, int, int *);
+  const Kern kerns[6] = {instance_eval_kernel<RHO_CONST, false>,   instance_eval_kernel<RHO_CONST, true>,
+                         instance_eval_kernel<RHO_NODERIV, false>, instance_eval_kernel<RHO_NODERIV, true>,
+                         instance_eval_kernel<RHO_EXP, false>,     instance_eval_kernel<RHO_EXP, true>};
+  const Kern kern = kerns[2 * rho_mode(a) + (a.jac_ff ? 1 : 0)];
   if (d->inst_smem > 48 * 1024) {
     std::lock_guard<std::mutex> lk(g_dev_mutex);
     if (d->inst_smem > g_inst_smem_granted[d->device]) {
-      for (auto k : {instance_eval_kernel<true, true>, instance_eval_kernel<true, false>,
-                     instance_eval_kernel<false, true>, instance_eval_kernel<false, false>})
+      for (Kern k : kerns)
         CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d->inst_smem));
       g_inst_smem_granted[d->device] = d->inst_smem;
     }

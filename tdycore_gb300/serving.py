@@ -268,8 +268,8 @@ class Server:
     them concurrently (``slots`` worker threads), ``cohort`` requests of one
     size class at most per worker (``cohort=1``: one handle per request)."""
 
-    def __init__(self, slots: int = 32, hbm_budget_bytes: float = 150e9, fp32: bool = True, dt: float = 3600.0,
-                 runner=None, footprint=footprint_bytes, clock=time.perf_counter, cohort: int = 16):
+    def __init__(self, slots: int = 8, hbm_budget_bytes: float = 150e9, fp32: bool = True, dt: float = 3600.0,
+                 runner=None, footprint=footprint_bytes, clock=time.perf_counter, cohort: int = 32):
         self.slots, self.budget, self.fp32, self.dt = slots, float(hbm_budget_bytes), fp32, dt
         self.cohort = max(1, cohort)
         if runner is None:
