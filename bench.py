@@ -306,6 +306,7 @@ def batched_config4(ninst=4096, sample=64, dt=3600.0):
                "max_rel_residual_device": stats["max_rel_residual"],
                "oracle_fp64": {"max_rel_residual": float(rel_o.max()),
                                "instances_meeting_1e-8": int(np.sum(meets)),
+                               "instances_not_meeting": [int(g) for g in np.nonzero(~meets)[0][:8]],
                                "instances_at_fp64_noise_floor": int(np.sum(at_floor & (rel_o > 1.01e-8)))}}
         return res, Ub
 
