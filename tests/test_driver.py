@@ -265,3 +265,30 @@ def test_driver_goldens_gpu(tmp_path):
     check_against_gold("transient-snes-mpfaof90-tdydriver",
                        parse_regression((tmp_path / "tdydriver.regression").read_text()))
     T.options_clear()
+
+
+@pytest.mark.gpu
+def test_infiltration_newton_gpu_matches_oracle():
+    """The 10x10x10 box started 60 kPa below hydrostatic (unsaturated): the
+    same host Newton around the GPU residual/Jacobian and around the oracle's
+    takes the same iterations on the steps that do real work and reaches the
+    same pressures."""
+    from tdycore_gb300.workloads import hydrostatic_box
+
+    T.options_clear()
+    t, U0, _ = hydrostatic_box()
+    t.setup()
+    t.set_dtime(1800.0)
+    o = Oracle(t.setup_view())
+    Ug, Uc = U0 - 60000.0, U0 - 60000.0
+    for step in range(3):
+        t.presolve(Ug)
+        o.snes_presolve(Uc, 1800.0)
+        rg = D.SNESNewtonLS().solve(t.snes_function, t.snes_jacobian, Ug.copy(), t.rowptr, t.colidx)
+        rc = D.SNESNewtonLS().solve(o.snes_function, o.snes_jacobian, Uc.copy(), t.rowptr, t.colidx)
+        assert rg.reason > 0 and rc.reason > 0
+        if step == 0:
+            assert rg.iterations == rc.iterations >= 5
+        Ug, Uc = rg.x, rc.x
+        assert np.max(np.abs(Ug - Uc) / np.abs(Uc)) < 1e-12
+    t.destroy()
