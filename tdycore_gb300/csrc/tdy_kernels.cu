@@ -668,6 +668,156 @@ __device__ __forceinline__ void canon_vertex_at(const DevArgs &a, int vc, int ti
   }
 }
 
+// Canonical vertex vc by a lane pair (h = lane parity; slot: the pair's
+// column of the block's ns shared rows), double-float Jacobian products.
+// Lane h computes rows 2h+i (x), 4+2h+i (y) and 8+2h+i (z), i = 0, 1: the x
+// and y rows of octants 4h..4h+3 and half of their z rows (the other half
+// comes from the partner by a shuffle); it writes R_v of octants 4h..4h+3 and
+// entries 4h..4h+3 (relative to the octant, column j ^ c) of every octant's
+// J_v.  Every value is formed by the operations of canon_vertex_at<RHO, true>
+// in the same order, so both give the same bits.  A pair holds half the live
+// state of one thread (the upwind cell data sit in shared memory), which
+// doubles the warps that hide the FP64 latency.
+constexpr int pair_shared_rows(int rho) { return 36 + 16 + (rho == 0 ? 0 : 8) + (rho == 2 ? 8 : 0); }
+template <int RHO>
+__device__ __forceinline__ void canon_vertex_pair(const DevArgs &a, int vc, int slot, int h, int ns) {
+  constexpr bool CONST_RHO = RHO != RHO_EXP;
+  // [36][ns]: w, E_up, E_dn per row; [8][ns] kr/mu and d(kr/mu)/dP per
+  // octant; rho/2 and d(rho/2)/dP per octant where the density varies
+  extern __shared__ double sh[];
+  double *s_lam = sh + 36 * ns, *s_dlam = s_lam + 8 * ns, *s_hr = s_dlam + 8 * ns, *s_hdr = s_hr + 8 * ns;
+  const unsigned pm = 3u << ((threadIdx.x & 31) & ~1);
+  const long long P = a.nCpad;
+  double p[8];
+#pragma unroll
+  for (int o = 0; o < 8; o++) {
+    const int cell = a.cellc[o * P + vc];
+    p[o] = a.P[cell];
+    if ((o >> 2) == h) {
+      s_lam[o * ns + slot] = a.lam[cell];
+      s_dlam[o * ns + slot] = a.dlam[cell];
+      if (RHO != RHO_CONST) s_hr[o * ns + slot] = a.hr[cell];
+      if (!CONST_RHO) s_hdr[o * ns + slot] = a.hdr[cell];
+    }
+  }
+  __syncwarp(pm);
+  double fx[2], fy[2], fz[2];
+#pragma unroll
+  for (int t = 0; t < 6; t++) {
+    const int axis = t >> 1, i = t & 1;
+    const int r = 4 * axis + 2 * h + i;
+    // octants of row r (canon_up, canon_dn) for this lane
+    const int u = h ? (axis == 0 ? 4 + 2 * i : axis == 1 ? 4 + i : 2 + i) : (axis == 0 ? 2 * i : i);
+    const int d = u + (1 << axis);
+    const double *T = a.Tc + (long long)(r * 8) * P + vc;
+    double TP = __dmul_rn(T[0], p[0]);
+#pragma unroll
+    for (int c = 1; c < 8; c++) TP = __fma_rn(T[c * P], p[c], TP);
+    const double G = a.G[a.facec[r * P + vc]];
+    const double den = RHO == RHO_CONST ? kRhoConst : __dadd_rn(s_hr[u * ns + slot], s_hr[d * ns + slot]);
+    const double q = __fma_rn(den, G, TP);
+    const bool fdn = dneg(q);
+    const int uw = fdn ? u : d;  // upwind octant
+    const double lm = s_lam[uw * ns + slot];
+    const double w = __dmul_rn(den, lm);
+    const double flux = -__dmul_rn(w, q);
+    (axis == 0 ? fx : axis == 1 ? fy : fz)[i] = flux;
+    if (a.needJ) {
+      const double dl = s_dlam[uw * ns + slot];
+      double eu, ed;
+      if (CONST_RHO) {
+        const double e = __dmul_rn(__dmul_rn(den, q), dl);
+        eu = fdn ? e : 0.0;
+        ed = fdn ? 0.0 : e;
+      } else {
+        const double dlu = fdn ? dl : 0.0, dld = fdn ? 0.0 : dl;
+        const double g2 = __fma_rn(den, G, q);
+        eu = __fma_rn(__dmul_rn(s_hdr[u * ns + slot], lm), g2, __dmul_rn(__dmul_rn(den, dlu), q));
+        ed = __fma_rn(__dmul_rn(s_hdr[d * ns + slot], lm), g2, __dmul_rn(__dmul_rn(den, dld), q));
+      }
+      sh[r * ns + slot] = w;
+      sh[(12 + r) * ns + slot] = eu;
+      sh[(24 + r) * ns + slot] = ed;
+    }
+  }
+  // z rows 8 + 2(1 - h) + i from the partner
+  double pz[2];
+#pragma unroll
+  for (int i = 0; i < 2; i++) pz[i] = __shfl_xor_sync(pm, fz[i], 1);
+  double *S = a.scratch;
+  if (a.needR) {
+    // octant o = 4h + ol: x row 2h + (ol >> 1), y row 4 + 2h + (ol & 1),
+    // z row 8 + ol; first touch from the x row, then y, then z (row order)
+#pragma unroll
+    for (int ol = 0; ol < 4; ol++) {
+      const double f1 = fx[ol >> 1], f2 = fy[ol & 1];
+      const double f3 = ((ol >> 1) == h) ? fz[ol & 1] : pz[ol & 1];
+      double Rv = (ol & 1) ? -f1 : f1;
+      Rv = (ol & 2) ? Rv - f2 : Rv + f2;
+      Rv = h ? Rv - f3 : Rv + f3;
+      S[64 * P + (4 * h + ol) * P + vc] = Rv;
+    }
+  }
+  if (!a.needJ) return;
+  __syncwarp(pm);
+#pragma unroll 1
+  for (int c = 0; c < 8; c++) {
+    // entries jj = 0..3 of this lane are entries j = 4h + jj of octant c
+    double wk[3], es[3], en[3], Tk[3][4];
+    int bw[3], mb[4];
+#pragma unroll
+    for (int jj = 0; jj < 4; jj++) mb[jj] = 0;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const int r = canon_row(c, k);
+      const bool up = canon_is_up(c, k);
+      wk[k] = sh[r * ns + slot];
+      bw[k] = d_bexp(wk[k]);
+      const double eu = sh[(12 + r) * ns + slot], ed = sh[(24 + r) * ns + slot];
+      es[k] = up ? eu : ed;  // E term of c itself (entry 0)
+      en[k] = up ? ed : eu;  // E term of the neighbour c ^ (1 << k) (entry 1 << k)
+      const double *T = a.Tc + (long long)(r * 8) * P + vc;
+#pragma unroll
+      for (int jj = 0; jj < 4; jj++) {
+        Tk[k][jj] = T[((4 * h + jj) ^ c) * P];
+        mb[jj] = max(mb[jj], bw[k] + d_bexp(Tk[k][jj]) - 1023);
+      }
+      if (k < 2) {
+        if (h == 0) {
+          mb[0] = max(mb[0], d_bexp(es[k]));
+          mb[1 << k] = max(mb[1 << k], d_bexp(en[k]));
+        }
+      } else {
+        mb[0] = max(mb[0], d_bexp(h ? en[2] : es[2]));  // entry 4 gets en[2]
+      }
+    }
+    ff acc[4];
+#pragma unroll
+    for (int jj = 0; jj < 4; jj++) acc[jj] = ff{0.0f, 0.0f};
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const bool up = canon_is_up(c, k);
+      ff wf = ff_split_scaled(wk[k], bw[k], 1023 - bw[k]);
+      const double e0 = h ? en[k] : es[k];
+      ff ef = ff_split_scaled(e0, d_bexp(e0), 1023 - mb[0]);
+      ff nf = k < 2 ? ff_split_scaled(en[k], d_bexp(en[k]), 1023 - mb[(1 << k) & 3]) : ff{0.0f, 0.0f};
+      if (up) {
+        wf = ff_neg(wf);
+        ef = ff_neg(ef);
+        nf = ff_neg(nf);
+      }
+#pragma unroll
+      for (int jj = 0; jj < 4; jj++)
+        ff_acc(acc[jj], ff_mul(wf, ff_split_scaled(Tk[k][jj], d_bexp(Tk[k][jj]), bw[k] - mb[jj])));
+      if (h == 0 || k == 2) ff_acc(acc[0], ef);
+      if (k < 2 && h == 0) ff_acc(acc[(1 << k) & 3], nf);
+    }
+    double *dst = S + ((long long)c * P + vc) * 8;
+#pragma unroll
+    for (int jj = 0; jj < 4; jj++) dst[(4 * h + jj) ^ c] = ff_to_d(acc[jj], mb[jj] - 1023);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // 3. other vertices.  Both forms below sum every Jacobian entry (c, b) of a
 // vertex block over the rows whose faces touch local cell c in row order,
@@ -855,6 +1005,21 @@ __global__ void __launch_bounds__(128) vertex_kernel(DevArgs a, int gen_blocks) 
   if ((int)blockIdx.x >= gen_blocks) {
     const int vc = a.vc0 + ((int)blockIdx.x - gen_blocks) * blockDim.x + threadIdx.x;
     if (vc < a.vc1) canon_vertex_at<RHO, FFJ>(a, vc, threadIdx.x);
+  } else {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g < a.ngen) generic_vertex_one(a, g);
+  }
+}
+
+// The same with a lane pair per canonical vertex (double-float Jacobian
+// products): a block of kPairThreads threads takes kPairThreads / 2 vertices.
+constexpr int kPairThreads = 128;
+template <int RHO>
+__global__ void __launch_bounds__(kPairThreads, 7) vertex_pair_kernel(DevArgs a, int gen_blocks) {
+  if ((int)blockIdx.x >= gen_blocks) {
+    const int slot = threadIdx.x >> 1, h = threadIdx.x & 1;
+    const int vc = a.vc0 + ((int)blockIdx.x - gen_blocks) * (kPairThreads / 2) + slot;
+    if (vc < a.vc1) canon_vertex_pair<RHO>(a, vc, slot, h, kPairThreads / 2);
   } else {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g < a.ngen) generic_vertex_one(a, g);
@@ -1554,6 +1719,19 @@ static int launch_vertices(const DevArgs &a, bool gen_warp, cudaStream_t st) {
   }
   const size_t canon_smem = 36 * 128 * sizeof(double);
   const int cb = (int)nblocks(a.vc1 - a.vc0, 128), gb = gen_warp ? 0 : (int)nblocks(a.ngen, 128);
+  if (a.jac_ff) {
+    const size_t pair_smem = (size_t)pair_shared_rows(rho_mode(a)) * (kPairThreads / 2) * sizeof(double);
+    const int pb = (int)nblocks(a.vc1 - a.vc0, kPairThreads / 2), pgb = gen_warp ? 0 : (int)nblocks(a.ngen, kPairThreads);
+    if (pb + pgb == 0) return 0;
+    const int rho = rho_mode(a);
+    if (rho == RHO_CONST)
+      vertex_pair_kernel<RHO_CONST><<<pb + pgb, kPairThreads, pair_smem, st>>>(a, pgb);
+    else if (rho == RHO_NODERIV)
+      vertex_pair_kernel<RHO_NODERIV><<<pb + pgb, kPairThreads, pair_smem, st>>>(a, pgb);
+    else
+      vertex_pair_kernel<RHO_EXP><<<pb + pgb, kPairThreads, pair_smem, st>>>(a, pgb);
+    return 0;
+  }
   if (cb + gb > 0) {
     const int rho = rho_mode(a);
     if (rho == RHO_CONST && a.jac_ff)
