@@ -784,9 +784,11 @@ def run_gpu(args, rank, world, local_rank):
         return world * nc * e2e_steps / el
 
     e2e_value = end_to_end(t)
+    e2e_out = (Rn.copy(), Jn.copy())  # the host-pointer call's last R and J (slab pipeline)
 
     # the same device loop and end-to-end call with FP64 Jacobian products
     R_main, J_main = dR.cpu().numpy(), dJ.cpu().numpy()
+    e2e_bits_equal = bool(np.array_equal(e2e_out[0], R_main) and np.array_equal(e2e_out[1], J_main))
     alt = None
     if args.jacobian_arithmetic != "FP64":
         t.destroy()
@@ -902,7 +904,8 @@ def run_gpu(args, rank, world, local_rank):
             "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": f"{n_cpu} full F+J evaluations ({cpu_s:.1f} s) of the same workload"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * nc,
-                    "d2h_bytes_per_step": 8 * (nc + nnz), "steps": e2e_steps},
+                    "d2h_bytes_per_step": 8 * (nc + nnz), "steps": e2e_steps,
+                    "R_J_equal_device_path": e2e_bits_equal},
             "gpu_launches": args.steps * launches,
             "parity_full_size": parity,
             "config1_newton": cfg1,

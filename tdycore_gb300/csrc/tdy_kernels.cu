@@ -46,6 +46,7 @@
 
 #include "tdy_arena.h"
 #include "tdy_device.h"
+#include "tdy_emit.h"
 #include "tdy_ff.h"
 
 namespace tdy {
@@ -134,6 +135,7 @@ struct DeviceState {
   // host-pointer evaluations in slabs of cells (see build_slabs): each slab's
   // rows of R and J go to host memory while the next slabs are evaluated
   struct Slab {
+    int e0, e1;        // cells whose state this slab computes (its vertices read up to e1)
     int c0, c1;        // cells
     int vc0, vc1;      // canonical vertices
     int g0, g1;        // other vertices (indices into gen_vertex)
@@ -144,6 +146,19 @@ struct DeviceState {
   std::vector<Slab> slabs;
   cudaStream_t copy_stream = nullptr;
   std::vector<cudaEvent_t> slab_ev;
+  // the slab pipeline as one graph for pinned host buffers, with what its
+  // nodes bake in (rebuilt when a call differs)
+  struct SlabKey {
+    int form = -1;
+    double dt = 0.0, shift = 0.0;
+    const double *U = nullptr, *Ut = nullptr;
+    double *R = nullptr, *J = nullptr;
+    bool operator==(const SlabKey &o) const {
+      return form == o.form && dt == o.dt && shift == o.shift && U == o.U && Ut == o.Ut && R == o.R && J == o.J;
+    }
+  };
+  cudaGraphExec_t slab_exec = nullptr;
+  SlabKey slab_key;
   // callers' streams that enqueued work on this handle, each with an event
   // recorded after its last enqueue: TDyDestroy waits for them before the
   // stream-ordered frees (which do not synchronise the device)
@@ -388,10 +403,12 @@ __device__ __forceinline__ void state_entity(const DevArgs &a, int i) {
   }
 }
 
-__global__ void __launch_bounds__(256) state_kernel(DevArgs a, int nchunks, int chunk_mul) {
+// entities [e0, e1) (cells below nc, then boundary faces)
+__global__ void __launch_bounds__(256) state_kernel(DevArgs a, int e0, int e1, int nchunks, int chunk_mul) {
   const int gw = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   if (gw >= nchunks) return;
-  state_entity(a, (int)(((long long)gw * chunk_mul) % nchunks) * 32 + (threadIdx.x & 31));
+  const int i = e0 + (int)(((long long)gw * chunk_mul) % nchunks) * 32 + (int)(threadIdx.x & 31);
+  if (i < e1) state_entity(a, i);
 }
 
 // Accumulation at the previous solution (TDyMPFAOSNESPreSolve,
@@ -1295,11 +1312,20 @@ static int note_stream(DeviceState *d, cudaStream_t st) {
 }
 
 // Slabs of the host-pointer evaluation, for a single extruded block (cells
-// numbered layer by layer): cells split at layer boundaries into up to four
-// slabs; a vertex belongs to the slab of the first cell that uses it, so the
-// cells of slab k need only vertices of slabs <= k.  The vertex and cell
+// numbered layer by layer): cells split at layer boundaries, the first slab
+// 1/kSlabFirst of the layers, each next one kSlabGrowth times the previous
+// up to 1/kSlabCap (a remainder below half a slab joins the last one).  The
+// copies of R and J to host memory run about 1.2x slower than the
+// evaluation, so once the first slab is evaluated the copy engine stays
+// busy; slabs much thinner than this cost more than they save, since every
+// launch lasts at least the latency of one block (about 30 us for the vertex
+// stage).  A vertex belongs to the slab of the first cell that uses it, so
+// the cells of slab k need only vertices of slabs <= k.  The vertex and cell
 // lists (ascending indices) must then run through the slabs in order, which
-// is checked: any other numbering leaves one slab (no pipelining).
+// is checked: any other numbering leaves one slab (no pipelining).  Slab k
+// also computes the state of the cells its vertices read beyond its own (the
+// layer above), up to e1.
+constexpr double kSlabFirst = 16, kSlabGrowth = 1.25, kSlabCap = 8;
 static void build_slabs(_p_TDy *t, DeviceState *d) {
   d->slabs.clear();
   if (t->mesh_blocks.size() != 1) return;
@@ -1307,10 +1333,18 @@ static void build_slabs(_p_TDy *t, DeviceState *d) {
   const Mesh &m = t->mesh;
   const MPFAOSetup &s = t->setup;
   const int nl = blk.nlayers, nc2 = blk.nc2;
-  const int K = std::min(4, nl / 4);
-  if (K < 2 || m.nc != nl * nc2) return;
-  std::vector<int> cut(K + 1);
-  for (int k = 0; k <= K; k++) cut[k] = (int)((long long)k * nl / K) * nc2;
+  if (nl < 8 || m.nc != nl * nc2) return;
+  const double cap = nl / kSlabCap;
+  std::vector<int> cut = {0};
+  int step = 1;
+  for (double size = nl / kSlabFirst, layer = 0; layer < nl; size = std::min(cap, size * kSlabGrowth)) {
+    step = std::max(1, (int)std::lround(size));
+    layer = std::min<double>(nl, layer + step);
+    cut.push_back((int)layer * nc2);
+  }
+  if (cut.size() > 2 && 2 * (cut[cut.size() - 1] - cut[cut.size() - 2]) < step * nc2) cut.erase(cut.end() - 2);
+  const int K = (int)cut.size() - 1;
+  if (K < 2) return;
   auto slab_of_cell = [&](int c) { return (int)(std::upper_bound(cut.begin(), cut.end(), c) - cut.begin()) - 1; };
   auto slab_of_vertex = [&](int v) { return slab_of_cell(m.vert_cells[m.vert_cell_off[v]]); };
   // b[k] = first list index in slab k or later; false if the slab decreases
@@ -1329,8 +1363,21 @@ static void build_slabs(_p_TDy *t, DeviceState *d) {
   if (!bounds(s.canon_vertex, slab_of_vertex, bc) || !bounds(s.gen_vertex, slab_of_vertex, bg) ||
       !bounds(s.sc_cells, slab_of_cell, bs) || !bounds(s.gc_cells, slab_of_cell, bgc))
     return;
+  int e_prev = 0;
   for (int k = 0; k < K; k++) {
     DeviceState::Slab sl;
+    int need = cut[k + 1];
+    auto reach = [&](const std::vector<int> &list, int b0, int b1) {
+      for (int i = b0; i < b1; i++) {
+        const int v = list[i];
+        for (int q = m.vert_cell_off[v]; q < m.vert_cell_off[v + 1]; q++) need = std::max(need, m.vert_cells[q] + 1);
+      }
+    };
+    reach(s.canon_vertex, bc[k], bc[k + 1]);
+    reach(s.gen_vertex, bg[k], bg[k + 1]);
+    sl.e0 = e_prev;
+    sl.e1 = k == K - 1 ? m.nc : std::max(std::min(need, m.nc), e_prev);
+    e_prev = sl.e1;
     sl.c0 = cut[k];
     sl.c1 = cut[k + 1];
     sl.vc0 = bc[k];
@@ -1633,6 +1680,7 @@ void device_destroy(_p_TDy *t) {
   }
   for (int k = 0; k < 4; k++)
     if (d->ev[k]) cudaEventDestroy(d->ev[k]);
+  if (d->slab_exec) cudaGraphExecDestroy(d->slab_exec);
   if (d->copy_stream) {
     cudaStreamSynchronize(d->copy_stream);
     pool_release(d->device, d->copy_stream, nullptr);
@@ -1695,11 +1743,12 @@ int device_presolve_host(_p_TDy *t, const double *Uprev) {
 
 // The four launches of one evaluation; events[] (5 entries, or null) bracket
 // them for the per-kernel timers.
-static int launch_state(const DevArgs &a, cudaStream_t st) {
-  const int nchunks = (int)nblocks(a.nc + a.nb, 32);
-  state_kernel<<<nblocks((long long)nchunks * 32, 256), 256, 0, st>>>(a, nchunks, chunk_multiplier(nchunks));
-  return 0;
+static void launch_state_range(const DevArgs &a, int e0, int e1, Emit &e) {
+  if (e1 <= e0) return;
+  const int nchunks = (int)nblocks(e1 - e0, 32);
+  e(state_kernel, nblocks((long long)nchunks * 32, 256), 256, 0, a, e0, e1, nchunks, chunk_multiplier(nchunks));
 }
+static void launch_state(const DevArgs &a, Emit &e) { launch_state_range(a, 0, a.nc + a.nb, e); }
 
 // Vertex stage over the vertices a names (gen_vertex/ngen, [vc0, vc1)).
 // gen_warp: mostly other vertices (e.g. prisms, whose valence-4 vertices are
@@ -1712,42 +1761,26 @@ static int rho_mode(const DevArgs &a) {
                                                    : RHO_NODERIV;
 }
 
-static int launch_vertices(const DevArgs &a, bool gen_warp, cudaStream_t st) {
-  if (gen_warp && a.ngen > 0) {
-    const size_t gen_smem = (size_t)kGenWarps * a.gen_warp_doubles * sizeof(double);
-    generic_vertex_kernel<<<nblocks(a.ngen, kGenWarps), 128, gen_smem, st>>>(a);
-  }
-  const size_t canon_smem = 36 * 128 * sizeof(double);
-  const int cb = (int)nblocks(a.vc1 - a.vc0, 128), gb = gen_warp ? 0 : (int)nblocks(a.ngen, 128);
+static void launch_vertices(const DevArgs &a, bool gen_warp, Emit &e) {
+  if (gen_warp && a.ngen > 0)
+    e(generic_vertex_kernel, nblocks(a.ngen, kGenWarps), 128, (size_t)kGenWarps * a.gen_warp_doubles * sizeof(double),
+      a);
+  const int rho = rho_mode(a);
   if (a.jac_ff) {
-    const size_t pair_smem = (size_t)pair_shared_rows(rho_mode(a)) * (kPairThreads / 2) * sizeof(double);
-    const int pb = (int)nblocks(a.vc1 - a.vc0, kPairThreads / 2), pgb = gen_warp ? 0 : (int)nblocks(a.ngen, kPairThreads);
-    if (pb + pgb == 0) return 0;
-    const int rho = rho_mode(a);
-    if (rho == RHO_CONST)
-      vertex_pair_kernel<RHO_CONST><<<pb + pgb, kPairThreads, pair_smem, st>>>(a, pgb);
-    else if (rho == RHO_NODERIV)
-      vertex_pair_kernel<RHO_NODERIV><<<pb + pgb, kPairThreads, pair_smem, st>>>(a, pgb);
-    else
-      vertex_pair_kernel<RHO_EXP><<<pb + pgb, kPairThreads, pair_smem, st>>>(a, pgb);
-    return 0;
+    const size_t smem = (size_t)pair_shared_rows(rho) * (kPairThreads / 2) * sizeof(double);
+    const int pb = (int)nblocks(a.vc1 - a.vc0, kPairThreads / 2), gb = gen_warp ? 0 : (int)nblocks(a.ngen, kPairThreads);
+    auto k = rho == RHO_CONST ? vertex_pair_kernel<RHO_CONST>
+             : rho == RHO_NODERIV ? vertex_pair_kernel<RHO_NODERIV>
+                                  : vertex_pair_kernel<RHO_EXP>;
+    e(k, pb + gb, kPairThreads, smem, a, gb);
+    return;
   }
-  if (cb + gb > 0) {
-    const int rho = rho_mode(a);
-    if (rho == RHO_CONST && a.jac_ff)
-      vertex_kernel<RHO_CONST, true><<<cb + gb, 128, canon_smem, st>>>(a, gb);
-    else if (rho == RHO_CONST)
-      vertex_kernel<RHO_CONST, false><<<cb + gb, 128, canon_smem, st>>>(a, gb);
-    else if (rho == RHO_NODERIV && a.jac_ff)
-      vertex_kernel<RHO_NODERIV, true><<<cb + gb, 128, canon_smem, st>>>(a, gb);
-    else if (rho == RHO_NODERIV)
-      vertex_kernel<RHO_NODERIV, false><<<cb + gb, 128, canon_smem, st>>>(a, gb);
-    else if (a.jac_ff)
-      vertex_kernel<RHO_EXP, true><<<cb + gb, 128, canon_smem, st>>>(a, gb);
-    else
-      vertex_kernel<RHO_EXP, false><<<cb + gb, 128, canon_smem, st>>>(a, gb);
-  }
-  return 0;
+  const size_t smem = 36 * 128 * sizeof(double);
+  const int cb = (int)nblocks(a.vc1 - a.vc0, 128), gb = gen_warp ? 0 : (int)nblocks(a.ngen, 128);
+  auto k = rho == RHO_CONST ? vertex_kernel<RHO_CONST, false>
+           : rho == RHO_NODERIV ? vertex_kernel<RHO_NODERIV, false>
+                                : vertex_kernel<RHO_EXP, false>;
+  e(k, cb + gb, 128, smem, a, gb);
 }
 
 // Cell stage over the cells a names (sc_cells/nS, gc_cells/ngc); gen_warp:
@@ -1758,15 +1791,12 @@ static size_t cell_smem_bytes(const DevArgs &a, bool gen_warp) {
 
 // (rows longer than 96 entries need more than 48 KB of dynamic shared
 // memory: device_setup opts in for the handle's device)
-static int launch_cells(const DevArgs &a, bool gen_warp, cudaStream_t st) {
-  const size_t cell_smem = cell_smem_bytes(a, gen_warp);
+static void launch_cells(const DevArgs &a, bool gen_warp, Emit &e) {
   const int sb = (int)nblocks(a.nS, 64), gcb = gen_warp ? 0 : (int)nblocks(a.ngc, 64);
-  if (sb + gcb > 0) cell_kernel<<<sb + gcb, 64, cell_smem, st>>>(a, sb);
-  if (gen_warp && a.ngc > 0) {
-    const size_t gcell_smem = (size_t)2 * kCellWarps * (size_t)a.max_row_nnz * sizeof(double);
-    generic_cell_kernel<<<nblocks(a.ngc, 2 * kCellWarps), 32 * kCellWarps, gcell_smem, st>>>(a);
-  }
-  return 0;
+  e(cell_kernel, sb + gcb, 64, cell_smem_bytes(a, gen_warp), a, sb);
+  if (gen_warp && a.ngc > 0)
+    e(generic_cell_kernel, nblocks(a.ngc, 2 * kCellWarps), 32 * kCellWarps,
+      (size_t)2 * kCellWarps * (size_t)a.max_row_nnz * sizeof(double), a);
 }
 
 static bool vertex_warp_form(const DevArgs &a) { return a.ngen > a.nC; }
@@ -1775,13 +1805,13 @@ static bool cell_warp_form(const DevArgs &a) { return a.ngc > a.nS; }
 // The stages of one evaluation; events[] (4 entries, or null) bracket them
 // for the per-kernel timers.
 static int launch_eval(const DevArgs &a, cudaStream_t st, cudaEvent_t *events) {
-  int ierr;
+  Emit e(st);
   if (events) CUDA_TRY(cudaEventRecord(events[0], st));
-  if ((ierr = launch_state(a, st))) return ierr;
+  launch_state(a, e);
   if (events) CUDA_TRY(cudaEventRecord(events[1], st));
-  if ((ierr = launch_vertices(a, vertex_warp_form(a), st))) return ierr;
+  launch_vertices(a, vertex_warp_form(a), e);
   if (events) CUDA_TRY(cudaEventRecord(events[2], st));
-  if ((ierr = launch_cells(a, cell_warp_form(a), st))) return ierr;
+  launch_cells(a, cell_warp_form(a), e);
   if (events) CUDA_TRY(cudaEventRecord(events[3], st));
   CUDA_TRY(cudaGetLastError());
   return 0;
@@ -1992,41 +2022,144 @@ int device_eval_dae_host(_p_TDy *t, double time, const double *U2, const double 
   return 0;
 }
 
+// The arguments of slab k: the vertices and cells of slab k only.
+static DevArgs slab_args(const DevArgs &a, const DeviceState::Slab &sl) {
+  DevArgs b = a;
+  b.gen_vertex = a.gen_vertex + sl.g0;
+  b.ngen = sl.g1 - sl.g0;
+  b.vc0 = sl.vc0;
+  b.vc1 = sl.vc1;
+  b.sc_cells = a.sc_cells + sl.s0;
+  b.sc_vc = a.sc_vc + sl.s0;  // structure of arrays, stride nSpad: the offset carries over
+  b.nS = sl.s1 - sl.s0;
+  b.gc_cells = a.gc_cells + sl.gc0;
+  b.ngc = sl.gc1 - sl.gc0;
+  return b;
+}
+
+static bool pinned(const void *p) {
+  if (!p) return true;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeHost;
+}
+
+// The slab pipeline as a graph: U (and U_t) to the device, the boundary
+// faces' state, then per slab the state of the cells its vertices read, its
+// vertex and cell stages, and its rows of J and R to host memory.  The state
+// of slab k waits for that of slab k-1 and, so that the first slab runs
+// alone, for the vertex stage of slab k-1; the vertex stage of slab k waits
+// for the state of slab k (so it sees every cell it reads); the cell stage of slab k waits
+// for its vertex stage only, so it runs beside the state and vertex stages of
+// slab k+1 (each stage writes entries no other running stage reads) and the
+// tail of one launch overlaps the next; the copies form a chain of their
+// own, each after its slab's cell stage, and run while the next slabs are
+// evaluated.  One launch replaces about ten driver calls per slab.
+static int build_slab_graph(_p_TDy *t, DeviceState *d, const DevArgs &a, const double *U, const double *Ut,
+                            double *R, double *J, cudaGraphExec_t *out) {
+  const size_t n = (size_t)t->mesh.nc;
+  cudaGraph_t g = nullptr;
+  CUDA_TRY(cudaGraphCreate(&g, 0));
+  cudaError_t err = cudaSuccess;
+  cudaGraphNode_t up[2] = {nullptr, nullptr}, join = nullptr, copy_last = nullptr;
+  int nup = 0;
+  err = cudaGraphAddMemcpyNode1D(&up[nup++], g, nullptr, 0, d->dU, U, sizeof(double) * n, cudaMemcpyHostToDevice);
+  if (err == cudaSuccess && Ut)
+    err = cudaGraphAddMemcpyNode1D(&up[nup++], g, nullptr, 0, d->dUt, Ut, sizeof(double) * n, cudaMemcpyHostToDevice);
+  if (err == cudaSuccess) err = cudaGraphAddEmptyNode(&join, g, up, nup);
+  Emit e(nullptr);
+  e.g = g;
+  e.last = join;
+  if (err == cudaSuccess) {
+    const bool vw = vertex_warp_form(a), cw = cell_warp_form(a);
+    const size_t K = d->slabs.size();
+    launch_state_range(a, a.nc, a.nc + a.nb, e);  // boundary faces
+    cudaGraphNode_t sprev = e.last, vprev = nullptr;
+    for (size_t k = 0; k < K && err == cudaSuccess && e.err == cudaSuccess; k++) {
+      const DeviceState::Slab &sl = d->slabs[k];
+      const DevArgs b = slab_args(a, sl);
+      // the state of slab k after that of slab k-1 and the vertex stage of
+      // slab k-1 (so the first slab runs alone), then its vertex stage
+      cudaGraphNode_t sdeps[2] = {sprev, vprev}, sjoin = nullptr;
+      err = cudaGraphAddEmptyNode(&sjoin, g, sdeps, vprev ? 2 : 1);
+      if (err != cudaSuccess) break;
+      e.last = sjoin;
+      launch_state_range(a, sl.e0, sl.e1, e);
+      sprev = e.last;
+      launch_vertices(b, vw, e);
+      vprev = e.last;
+      launch_cells(b, cw, e);
+      if (e.err != cudaSuccess) break;
+      cudaGraphNode_t deps[2] = {e.last, copy_last}, nj = nullptr;
+      err = cudaGraphAddMemcpyNode1D(&nj, g, deps, copy_last ? 2 : 1, J + sl.j0, d->dJ + sl.j0,
+                                     sizeof(double) * (size_t)(sl.j1 - sl.j0), cudaMemcpyDeviceToHost);
+      copy_last = nj;
+      if (err == cudaSuccess && R) {
+        cudaGraphNode_t dr[2] = {e.last, copy_last}, nr = nullptr;
+        err = cudaGraphAddMemcpyNode1D(&nr, g, dr, 2, R + sl.c0, d->dR + sl.c0, sizeof(double) * (size_t)(sl.c1 - sl.c0),
+                                       cudaMemcpyDeviceToHost);
+        copy_last = nr;
+      }
+    }
+  }
+  if (err == cudaSuccess) err = e.err;
+  if (err == cudaSuccess) err = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  if (err != cudaSuccess) return set_error(TDY_ERR_GPU, "slab graph: %s", cudaGetErrorString(err));
+  return 0;
+}
+
 int device_eval_host(_p_TDy *t, int form, double time, const double *U, const double *Ut, double shift, double *R,
                      double *J) {
   DeviceState *d = t->dev;
   const size_t n = (size_t)t->mesh.nc;
-  CUDA_TRY(cudaMemcpyAsync(d->dU, U, sizeof(double) * n, cudaMemcpyHostToDevice, d->stream));
-  if (Ut) CUDA_TRY(cudaMemcpyAsync(d->dUt, Ut, sizeof(double) * n, cudaMemcpyHostToDevice, d->stream));
   if (d->slabs.size() > 1 && J && !d->timers) {
-    // slab by slab: the vertex and cell stages of slab k, then its rows of R
-    // and J to host memory on the copy stream while slab k+1 is evaluated
-    // (the same launches, split; the same bits)
+    // slab by slab (build_slabs): the same launches, split; the same bits
     DevArgs a;
     int ierr = eval_args(t, form, d->dU, Ut ? d->dUt : nullptr, shift, R ? d->dR : nullptr, d->dJ, &a);
     if (ierr) return ierr;
-    if (!d->copy_stream) {  // first host-pointer Jacobian call of this handle
+    DeviceState::SlabKey key;
+    key.form = form;
+    key.dt = a.dt;
+    key.shift = a.shift;
+    key.U = U;
+    key.Ut = Ut;
+    key.R = R;
+    key.J = J;
+    if (d->slab_exec && !(key == d->slab_key)) {
+      CUDA_TRY(cudaGraphExecDestroy(d->slab_exec));
+      d->slab_exec = nullptr;
+    }
+    if (!d->slab_exec && pinned(U) && pinned(Ut) && pinned(R) && pinned(J)) {
+      if ((ierr = build_slab_graph(t, d, a, U, Ut, R, J, &d->slab_exec))) return ierr;
+      d->slab_key = key;
+    }
+    if (d->slab_exec) {
+      CUDA_TRY(cudaGraphLaunch(d->slab_exec, d->stream));
+      CUDA_TRY(cudaStreamSynchronize(d->stream));
+      return 0;
+    }
+    // pageable host buffers: the same pipeline on two streams
+    CUDA_TRY(cudaMemcpyAsync(d->dU, U, sizeof(double) * n, cudaMemcpyHostToDevice, d->stream));
+    if (Ut) CUDA_TRY(cudaMemcpyAsync(d->dUt, Ut, sizeof(double) * n, cudaMemcpyHostToDevice, d->stream));
+    if (!d->copy_stream) {  // first such call of this handle
       if ((ierr = pool_stream(&d->copy_stream))) return ierr;
       d->slab_ev.assign(d->slabs.size(), nullptr);
       for (cudaEvent_t &e : d->slab_ev)
         if ((ierr = pool_event(&e))) return ierr;
     }
     const bool vw = vertex_warp_form(a), cw = cell_warp_form(a);
-    if ((ierr = launch_state(a, d->stream))) return ierr;
+    Emit e(d->stream);
+    launch_state_range(a, a.nc, a.nc + a.nb, e);  // boundary faces
     for (size_t k = 0; k < d->slabs.size(); k++) {
       const DeviceState::Slab &sl = d->slabs[k];
-      DevArgs b = a;
-      b.gen_vertex = a.gen_vertex + sl.g0;
-      b.ngen = sl.g1 - sl.g0;
-      b.vc0 = sl.vc0;
-      b.vc1 = sl.vc1;
-      b.sc_cells = a.sc_cells + sl.s0;
-      b.sc_vc = a.sc_vc + sl.s0;  // structure of arrays, stride nSpad: the offset carries over
-      b.nS = sl.s1 - sl.s0;
-      b.gc_cells = a.gc_cells + sl.gc0;
-      b.ngc = sl.gc1 - sl.gc0;
-      if ((ierr = launch_vertices(b, vw, d->stream))) return ierr;
-      if ((ierr = launch_cells(b, cw, d->stream))) return ierr;
+      const DevArgs b = slab_args(a, sl);
+      launch_state_range(a, sl.e0, sl.e1, e);
+      launch_vertices(b, vw, e);
+      launch_cells(b, cw, e);
       CUDA_TRY(cudaEventRecord(d->slab_ev[k], d->stream));
       CUDA_TRY(cudaStreamWaitEvent(d->copy_stream, d->slab_ev[k], 0));
       CUDA_TRY(cudaMemcpyAsync(J + sl.j0, d->dJ + sl.j0, sizeof(double) * (size_t)(sl.j1 - sl.j0),
@@ -2040,6 +2173,8 @@ int device_eval_host(_p_TDy *t, int form, double time, const double *U, const do
     CUDA_TRY(cudaStreamSynchronize(d->stream));
     return 0;
   }
+  CUDA_TRY(cudaMemcpyAsync(d->dU, U, sizeof(double) * n, cudaMemcpyHostToDevice, d->stream));
+  if (Ut) CUDA_TRY(cudaMemcpyAsync(d->dUt, Ut, sizeof(double) * n, cudaMemcpyHostToDevice, d->stream));
   int ierr = device_eval(t, form, time, d->dU, Ut ? d->dUt : nullptr, shift, R ? d->dR : nullptr, J ? d->dJ : nullptr,
                          d->stream);
   if (ierr) return ierr;

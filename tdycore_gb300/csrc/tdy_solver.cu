@@ -33,6 +33,7 @@
 
 #include "tdy_arena.h"
 #include "tdy_device.h"
+#include "tdy_emit.h"
 
 namespace tdy {
 
@@ -46,47 +47,6 @@ namespace {
   } while (0)
 
 inline unsigned nblk(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
-
-// Kernel launches of the solver go through an Emit: straight to its stream,
-// or, while a graph is being built, as the next kernel node of a chain in
-// that graph (the explicit graph API: the kernel's arguments are converted
-// to its parameter types and copied into the node).  Empty grids launch
-// nothing in either mode.
-struct Emit {
-  cudaStream_t st = nullptr;
-  cudaGraph_t g = nullptr;
-  cudaGraphNode_t last = nullptr;
-  cudaError_t err = cudaSuccess;
-  explicit Emit(cudaStream_t s) : st(s) {}
-  template <class... P, class... A>
-  void operator()(void (*k)(P...), unsigned grid, unsigned block, size_t smem, A... args) {
-    static_assert(sizeof...(P) == sizeof...(A), "kernel argument count");
-    if (grid == 0) return;
-    if (!g) {
-      k<<<grid, block, smem, st>>>(args...);
-      return;
-    }
-    if (err != cudaSuccess) return;
-    std::tuple<P...> vals(args...);
-    add_node((void *)k, grid, block, smem, vals, std::index_sequence_for<P...>{});
-  }
-
- private:
-  template <class Tup, size_t... I>
-  void add_node(void *fn, unsigned grid, unsigned block, size_t smem, Tup &vals, std::index_sequence<I...>) {
-    void *ptrs[sizeof...(I) > 0 ? sizeof...(I) : 1] = {(void *)&std::get<I>(vals)...};
-    cudaKernelNodeParams p = {};
-    p.func = fn;
-    p.gridDim = dim3(grid);
-    p.blockDim = dim3(block);
-    p.sharedMemBytes = (unsigned)smem;
-    p.kernelParams = ptrs;
-    p.extra = nullptr;
-    cudaGraphNode_t n = nullptr;
-    err = cudaGraphAddKernelNode(&n, g, last ? &last : nullptr, last ? 1 : 0, &p);
-    if (err == cudaSuccess) last = n;
-  }
-};
 
 // per-instance scalars, [slot][nseg]
 enum { S_RHO = 0, S_ALPHA, S_OMEGA, S_BETA, S_BNORM2, S_T1, S_T2, S_HALF, S_NSCAL };

@@ -98,6 +98,33 @@ def test_deterministic_and_device_entry_point():
     assert np.array_equal(dJ.cpu().numpy(), J1)
 
 
+def test_pinned_host_buffers_slab_graph():
+    """Pinned host buffers take the slab pipeline as one graph: the same bits
+    as pageable buffers and the device entry point, and a changed dt (which
+    the graph bakes in) gives a fresh graph with the new step's values."""
+    import torch
+
+    t, o, U, Uprev, _ = _setup("spe10_small")
+    t.set_dtime(DT)
+    t.presolve(Uprev)
+    R1, J1 = t.snes_function_jacobian(U)
+    Up = torch.tensor(U, dtype=torch.float64).pin_memory()
+    Rp = torch.full((t.ncells,), np.nan, dtype=torch.float64).pin_memory()
+    Jp = torch.full((t.nnz,), np.nan, dtype=torch.float64).pin_memory()
+    for _ in range(2):
+        t.snes_function_jacobian(Up.numpy(), Rp.numpy(), Jp.numpy())
+        assert np.array_equal(Rp.numpy(), R1) and np.array_equal(Jp.numpy(), J1)
+    t.set_dtime(DT / 4)
+    t.presolve(Uprev)
+    R2, J2 = t.snes_function_jacobian(U)
+    t.snes_function_jacobian(Up.numpy(), Rp.numpy(), Jp.numpy())
+    assert np.array_equal(Rp.numpy(), R2) and np.array_equal(Jp.numpy(), J2)
+    assert not np.array_equal(R2, R1)
+    o.snes_presolve(Uprev, DT / 4)
+    Rr, Rm = o.snes_function(U, with_mag=True)
+    assert_close(Rp.numpy(), Rr, Rm, R_TOL, "pinned slab graph residual")
+
+
 def test_jacobian_is_derivative_of_residual():
     """Central differences of the GPU residual against the GPU Jacobian."""
     t, o, U, Uprev, _ = _setup("spe10_small")
