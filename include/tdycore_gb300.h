@@ -222,7 +222,9 @@ typedef struct {
   int max_it;          /* Newton iterations (default 50, as PETSc SNES) */
   int linear_fp32;     /* 1: FP32 Jacobian and inner solve (default); 0: FP64 */
   double linear_rtol;  /* BiCGStab relative tolerance per instance (default 1e-6) */
-  int linear_max_it;   /* BiCGStab iterations per Newton iteration (default 400) */
+  int linear_max_it;   /* BiCGStab iterations per Newton iteration (default 400); an FP32 inner
+                          solve stops after a quarter of them (at least 20) and, if not converged
+                          by then, that instance's solve is redone in FP64 */
   double stol;         /* step tolerance: converged when ||step|| < stol ||U|| per instance
                           (PETSc's CONVERGED_SNORM_RELATIVE; default 1e-8) */
   int precond;         /* TDY_PRECOND_LINES (default) or TDY_PRECOND_CLUSTERS */
@@ -233,6 +235,9 @@ typedef struct {
   int fp32_max_it;     /* with linear_fp32: Newton iterations with the FP32 inner solve, FP64 after
                           (an instance still iterating then stalls on FP32 directions; default 8,
                           negative: FP32 throughout) */
+  int spmv_threads;    /* threads per row of the inner solve's sparse products: 0 (default) timed
+                          on the process's first solve; 1, 2, 4 or 8.  Every choice gives the same
+                          bits (each row is summed in 8 phases added by a fixed tree) */
 } TDyNewtonOptions;
 /* Inner-solve schedules.  TILE: every kernel of a BiCGStab iteration runs over
  * all cells of the batch, instances masked as they converge (one iteration is
@@ -270,6 +275,14 @@ typedef struct {
   int fp64_fallback;            /* 1 if Newton went past fp32_max_it and finished with FP64 inner solves */
   int eval_schedule;            /* evaluation of every instance: 0 three-stage launches, 1 one CTA per
                                    instance (timed on the handle's first evaluation; the same bits) */
+  double eval_s;                /* seconds on the solve's stream in F+J evaluations (line-search trials
+                                   included) */
+  double precond_s;             /* ... in Jacobian copies to the inner solve's precision and
+                                   preconditioner set-ups */
+  double krylov_s;              /* ... in BiCGStab iterations (schedule tuning on a size class's first
+                                   solve included) */
+  int fp64_inner_redo;          /* FP32 inner solves that ran out of iterations and were redone in FP64
+                                   (instances x Newton iterations) */
 } TDyNewtonStats;
 TDyErrorCode TDyNewtonOptionsDefault(TDyNewtonOptions *o);
 TDyErrorCode TDyGetNumInstances(TDy tdy, int *n);

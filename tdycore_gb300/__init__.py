@@ -68,7 +68,8 @@ class TDyMPFAOSetupView(ctypes.Structure):
 class NewtonOptions(ctypes.Structure):
     _fields_ = [("rtol", c_double), ("atol", c_double), ("max_it", c_int), ("linear_fp32", c_int),
                 ("linear_rtol", c_double), ("linear_max_it", c_int), ("stol", c_double), ("precond", c_int),
-                ("cluster_threshold", c_double), ("schedule", c_int), ("fp32_max_it", c_int)]
+                ("cluster_threshold", c_double), ("schedule", c_int), ("fp32_max_it", c_int),
+                ("spmv_threads", c_int)]
 
 
 PRECOND_LINES, PRECOND_CLUSTERS = 0, 1
@@ -80,7 +81,8 @@ class NewtonStats(ctypes.Structure):
                 ("ninstances", c_int), ("max_rel_residual", c_double), ("step_converged", c_int),
                 ("precond_used", c_int), ("clusters", c_int), ("cluster_cells", c_int),
                 ("cluster_cells_diagonal", c_int), ("block_instances", c_int), ("block_max_cells", c_longlong),
-                ("fp64_fallback", c_int), ("eval_schedule", c_int)]
+                ("fp64_fallback", c_int), ("eval_schedule", c_int), ("eval_s", c_double), ("precond_s", c_double),
+                ("krylov_s", c_double), ("fp64_inner_redo", c_int)]
 
 
 def _sig(name, *args):
@@ -635,13 +637,14 @@ class TDy:
 
     def backward_euler_step_device(self, dU, dt, rtol=1e-8, atol=0.0, max_it=50, fp32=True, linear_rtol=1e-6,
                                    linear_max_it=400, stol=1e-8, stream=None, precond="lines",
-                                   cluster_threshold=0.05, schedule="auto", fp32_max_it=8):
+                                   cluster_threshold=0.05, schedule="auto", fp32_max_it=8, spmv_threads=0):
         """One backward-Euler step of every instance with the device Newton
         solver; dU (device float64 tensor, ncells) holds U_n and receives
         U_{n+1}.  precond: "lines" or "clusters" (TDY_PRECOND_*); schedule:
         "auto", "tile" or "block" (TDY_SCHEDULE_*, the same bits); with
         fp32, inner solves switch to FP64 after fp32_max_it Newton iterations
-        (negative: never).  Returns
+        (negative: never); spmv_threads: threads per row of the inner solve's
+        sparse products (0: timed; 1, 2, 4, 8: the same bits).  Returns
         (stats dict, per-instance Newton iterations, per-instance final
         ||F||/||F_0||)."""
         o = NewtonOptions()
@@ -652,6 +655,7 @@ class TDy:
         o.cluster_threshold = cluster_threshold
         o.schedule = {"auto": SCHEDULE_AUTO, "tile": SCHEDULE_TILE, "block": SCHEDULE_BLOCK}[schedule]
         o.fp32_max_it = fp32_max_it
+        o.spmv_threads = spmv_threads
         st = NewtonStats()
         ni = self.num_instances()
         its = np.zeros(ni, dtype=np.int32)

@@ -1046,6 +1046,7 @@ TDyErrorCode TDyNewtonOptionsDefault(TDyNewtonOptions *o) {
   o->cluster_threshold = 0.05;
   o->schedule = TDY_SCHEDULE_AUTO;
   o->fp32_max_it = 8;
+  o->spmv_threads = 0;
   return 0;
 }
 TDyErrorCode TDySetActiveInstances(TDy tdy, int ninstances, const int *active) {
@@ -1090,7 +1091,9 @@ TDyErrorCode TDyBackwardEulerStepDevice(TDy tdy, double dt, double *dU, const TD
   if (o.max_it < 0 || o.linear_max_it < 1 || !(o.rtol >= 0.0) || !(o.linear_rtol > 0.0) ||
       (o.precond != TDY_PRECOND_LINES && o.precond != TDY_PRECOND_CLUSTERS) ||
       (o.precond == TDY_PRECOND_CLUSTERS && !(o.cluster_threshold > 0.0)) ||
-      (o.schedule != TDY_SCHEDULE_AUTO && o.schedule != TDY_SCHEDULE_TILE && o.schedule != TDY_SCHEDULE_BLOCK))
+      (o.schedule != TDY_SCHEDULE_AUTO && o.schedule != TDY_SCHEDULE_TILE && o.schedule != TDY_SCHEDULE_BLOCK) ||
+      (o.spmv_threads != 0 && o.spmv_threads != 1 && o.spmv_threads != 2 && o.spmv_threads != 4 &&
+       o.spmv_threads != 8))
     return set_error(TDY_ERR_ARG_OUTOFRANGE, "TDyBackwardEulerStepDevice: invalid options");
   return device_be_solve(tdy, dt, dU, o, stats, inst_iterations, inst_rel_residual, stream);
 }

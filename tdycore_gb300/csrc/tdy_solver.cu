@@ -62,6 +62,7 @@ struct Krylov {
   size_t clu_cap = 0;                                  // elements of clu
   cudaGraphExec_t graph = nullptr;
   int graph_precond = -1;  // preconditioner the graph was built with
+  int graph_tpr = 0;       // spmv threads per row the graph was built with
   int tpr = 0;  // spmv threads per row (autotuned)
 };
 
@@ -104,6 +105,9 @@ struct SolverState {
   // 1 instance schedule (timed on the first evaluation; the same bits)
   int eval_mode = -1;
   double eval_ms[2] = {0.0, 0.0};
+  // phase timers on the solve's stream: evaluation, Jacobian cast and
+  // preconditioner set-up, Krylov iterations (events of the current phase)
+  cudaEvent_t tev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   std::vector<long long> h_inst_cells;
   // device memory: stream-ordered on the handle's stream (allocated there and
   // synchronised at init; freed there when the solver is destroyed, after
@@ -111,6 +115,8 @@ struct SolverState {
   cudaStream_t st = nullptr;
   std::vector<void *> allocs;
   ~SolverState() {
+    for (cudaEvent_t e : tev)
+      if (e) cudaEventDestroy(e);
     for (Krylov *k : {&k32, &k64}) {
       if (k->graph) cudaGraphExecDestroy(k->graph);
       if (k->clu) dmem_free(k->clu, st);
@@ -183,6 +189,12 @@ __global__ void cast_kernel(long long n, const double *a, T *b) {
   if (i < n) b[i] = (T)a[i];
 }
 
+// the cells of the flagged instances: b = (float)a
+__global__ void cast_masked_kernel(int n, const int *cell_seg, const int *flag, const double *a, float *b) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && flag[cell_seg[i]]) b[i] = (float)a[i];
+}
+
 // Per-instance dot products in two deterministic passes: one block per chunk
 // of at most kChunk cells (chunks counted from each instance's first cell, so
 // an instance is reduced the same way alone and in a batch), then one thread
@@ -230,16 +242,42 @@ __global__ void chunk_sum_kernel(int nseg, const int *seg_chunk, const double *p
 }
 
 // y = A x over the CSR pattern with TPR threads per row
+// One row of A x by TPR lanes (1, 2, 4 or 8) with the same bits for every
+// TPR: the row's entries are split into 8 phases (entry k of the row in
+// phase k mod 8), each phase summed by one FMA chain in entry order, and the
+// 8 phase sums added by a fixed tree, ((P0+P4) + (P2+P6)) + ((P1+P5) +
+// (P3+P7)).  Lane l holds phases l, l+TPR, ...; the tree levels whose pairs
+// lie in one lane are added in registers, the others by shuffles, so the
+// lane split can be tuned for speed without changing any result.  Lane 0
+// returns the row's value.
+template <class T, int TPR>
+__device__ __forceinline__ T row_dot(bool valid, int k0, int k1, int lane, const int *colidx, const T *A, const T *x) {
+  constexpr int NP = 8 / TPR;
+  T P[NP];
+#pragma unroll
+  for (int q = 0; q < NP; q++) {
+    T acc = 0;
+    if (valid)
+      for (int k = k0 + lane + TPR * q; k < k1; k += 8) acc = e_fma(A[k], x[colidx[k]], acc);
+    P[q] = acc;
+  }
+#pragma unroll
+  for (int o = 4; o >= TPR; o >>= 1) {  // pairs (p, p + o) within the lane: q and q + o / TPR
+#pragma unroll
+    for (int q = 0; q < o / TPR; q++) P[q] = e_add(P[q], P[q + o / TPR]);
+  }
+  T acc = P[0];
+#pragma unroll
+  for (int o = TPR / 2; o > 0; o >>= 1) acc = e_add(acc, __shfl_down_sync(0xffffffffu, acc, o, TPR));
+  return acc;
+}
+
 template <class T, int TPR>
 __global__ void __launch_bounds__(256) spmv_kernel(int n, const int *rowptr, const int *colidx, const T *A, const T *x,
                                                    T *y) {
   const long long gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int row = (int)(gt / TPR), lane = (int)(gt % TPR);
-  T acc = 0;
-  if (row < n)
-    for (int k = rowptr[row] + lane; k < rowptr[row + 1]; k += TPR) acc = e_fma(A[k], x[colidx[k]], acc);
-#pragma unroll
-  for (int o = TPR / 2; o > 0; o >>= 1) acc = e_add(acc, __shfl_down_sync(0xffffffffu, acc, o, TPR));
+  const T acc = row_dot<T, TPR>(row < n, row < n ? rowptr[row] : 0, row < n ? rowptr[row + 1] : 0, lane, colidx, A, x);
   if (row < n && lane == 0) y[row] = acc;
 }
 
@@ -458,18 +496,15 @@ __device__ __forceinline__ void block_dot(int i0, int i1, const TA *a, const TB 
   if (out2) *out2 = tot2;
 }
 
-// y = A x over rows [c0, c1): spmv_kernel's lane split and shuffle order
+// y = A x over rows [c0, c1): the row sums of spmv_kernel (row_dot)
 template <class T, int TPR>
 __device__ __forceinline__ void block_spmv(int c0, int c1, const int *rowptr, const int *colidx, const T *A,
                                            const T *x, T *y) {
   const int nrow = c1 - c0;
   for (int base = 0; base < nrow * TPR; base += kBlockThreads) {
     const int gt = base + (int)threadIdx.x, rl = gt / TPR, lane = gt % TPR, row = c0 + rl;
-    T acc = 0;
-    if (rl < nrow)
-      for (int k = rowptr[row] + lane; k < rowptr[row + 1]; k += TPR) acc = e_fma(A[k], x[colidx[k]], acc);
-#pragma unroll
-    for (int o = TPR / 2; o > 0; o >>= 1) acc = e_add(acc, __shfl_down_sync(0xffffffffu, acc, o, TPR));
+    const T acc = row_dot<T, TPR>(rl < nrow, rl < nrow ? rowptr[row] : 0, rl < nrow ? rowptr[row + 1] : 0, lane,
+                                  colidx, A, x);
     if (rl < nrow && lane == 0) y[row] = acc;
   }
 }
@@ -747,6 +782,9 @@ int spmv(SolverState *s, const Krylov &k, const T *x, T *y, Emit &e) {
     case 1:
       e(spmv_kernel<T, 1>, g, 256, 0, s->n, (const int *)s->rowptr, (const int *)s->colidx, A, x, y);
       break;
+    case 2:
+      e(spmv_kernel<T, 2>, g, 256, 0, s->n, (const int *)s->rowptr, (const int *)s->colidx, A, x, y);
+      break;
     case 4:
       e(spmv_kernel<T, 4>, g, 256, 0, s->n, (const int *)s->rowptr, (const int *)s->colidx, A, x, y);
       break;
@@ -840,14 +878,18 @@ int krylov_alloc(SolverState *s, Krylov &k, cudaStream_t st) {
 }
 
 // Picks the spmv threads per row by timing the candidates on the first solve
-// of the process; the choice is then kept for every handle, so an instance
-// gets the same bits alone and inside a batch (the threads per row set the
-// summation order).
+// of the process and keeps the choice for every later handle (a server's
+// handles skip the timing); options.spmv_threads forces one.  The results do
+// not depend on it (row_dot).
 std::mutex g_tpr_mutex;
 int g_tpr[2] = {0, 0};  // float, double
 
 template <class T>
-int autotune_spmv(SolverState *s, Krylov &k, cudaStream_t st) {
+int autotune_spmv(SolverState *s, Krylov &k, int forced, cudaStream_t st) {
+  if (forced > 0) {
+    k.tpr = forced;
+    return 0;
+  }
   if (k.tpr) return 0;
   std::lock_guard<std::mutex> lk(g_tpr_mutex);
   int &cached = g_tpr[sizeof(T) == sizeof(double) ? 1 : 0];
@@ -861,7 +903,7 @@ int autotune_spmv(SolverState *s, Krylov &k, cudaStream_t st) {
   float best = 1e30f;
   int best_tpr = 1;
   Emit em(st);
-  for (int tpr : {1, 4, 8}) {
+  for (int tpr : {1, 2, 4, 8}) {
     k.tpr = tpr;
     spmv<T>(s, k, (const T *)k.b, (T *)k.v, em);  // warm-up
     cudaEventRecord(e0, st);
@@ -1070,6 +1112,9 @@ int solve_scheduled(SolverState *s, Krylov &k, const TDyNewtonOptions &o, double
       case 1:
         ierr = launch_block<T, 1>(s, k, o, tol2, st);
         break;
+      case 2:
+        ierr = launch_block<T, 2>(s, k, o, tol2, st);
+        break;
       case 4:
         ierr = launch_block<T, 4>(s, k, o, tol2, st);
         break;
@@ -1163,21 +1208,23 @@ int linear_solve(SolverState *s, Krylov &k, const TDyNewtonOptions &o, cudaStrea
                  std::vector<int> &inst_lin_its) {
   int ierr;
   if ((ierr = krylov_alloc<T>(s, k, st))) return ierr;
-  if ((ierr = autotune_spmv<T>(s, k, st))) return ierr;  // uses b and v as scratch before they are set
+  if ((ierr = autotune_spmv<T>(s, k, o.spmv_threads, st))) return ierr;  // uses b and v as scratch before they are set
   const int n = s->n, ns = s->nseg;
+  SCUDA(cudaEventRecord(s->tev[2], st));
   cast_kernel<T><<<nblk(s->nnz, 256), 256, 0, st>>>(s->nnz, s->J, (T *)k.Jv);
   s->precond_used = TDY_PRECOND_LINES;
   if (o.precond == TDY_PRECOND_CLUSTERS && (ierr = cluster_setup<T>(s, k, o.cluster_threshold, st))) return ierr;
   if (s->precond_used == TDY_PRECOND_LINES)
     line_factor_kernel<T><<<nblk(s->nlines, 128), 128, 0, st>>>(s->nlines, s->line_off, s->pos_d, s->pos_lo,
                                                                  s->pos_hi, s->J, (T *)k.la, (T *)k.lcp, (T *)k.linv);
+  SCUDA(cudaEventRecord(s->tev[3], st));
   const double tol2 = o.linear_rtol * o.linear_rtol;
   // The graph of one iteration is built with the explicit graph API, not by
   // stream capture: a capture is invalidated by device-wide operations that
   // other threads issue meanwhile (a cudaFree, a device synchronisation),
   // which a server running many handles at once cannot rule out.  The cluster
   // launches depend on this solve's cluster count: rebuild for every solve.
-  if (!k.graph || s->linear_rtol != o.linear_rtol || k.graph_precond != s->precond_used ||
+  if (!k.graph || s->linear_rtol != o.linear_rtol || k.graph_precond != s->precond_used || k.graph_tpr != k.tpr ||
       s->precond_used == TDY_PRECOND_CLUSTERS) {
     if (k.graph) cudaGraphExecDestroy(k.graph);
     k.graph = nullptr;
@@ -1194,6 +1241,7 @@ int linear_solve(SolverState *s, Krylov &k, const TDyNewtonOptions &o, cudaStrea
       return set_error(TDY_ERR_GPU, "BiCGStab iteration graph: %s", cudaGetErrorString(e));
     }
     k.graph_precond = s->precond_used;
+    k.graph_tpr = k.tpr;
     s->linear_rtol = o.linear_rtol;
   }
   std::vector<int> its(ns);
@@ -1209,6 +1257,7 @@ int linear_solve(SolverState *s, Krylov &k, const TDyNewtonOptions &o, cudaStrea
       return ierr;
   }
   if ((ierr = solve_scheduled<T>(s, k, o, tol2, thr, st, its))) return ierr;
+  SCUDA(cudaEventRecord(s->tev[4], st));
   for (int v : its) *lin_total += v;
   inst_lin_its = its;
   return 0;
@@ -1220,6 +1269,7 @@ int solver_init(_p_TDy *t) {
   SolverState *s = new SolverState();
   t->solver = s;
   s->st = (cudaStream_t)device_default_stream(t);
+  for (cudaEvent_t &e : s->tev) SCUDA(cudaEventCreate(&e));
   s->n = t->mesh.nc;
   s->nnz = (int)su.colidx.size();
   // instances: the mesh blocks; lines: the columns of each block, bottom to top
@@ -1317,6 +1367,17 @@ void device_solver_destroy(_p_TDy *t) {
 
 int device_num_instances(_p_TDy *t) { return (int)t->mesh_blocks.size(); }
 
+// the last linear_solve's set-up and Krylov times (ms), once its events completed
+static int add_linear_times(SolverState *s, double *prec, double *kry) {
+  SCUDA(cudaEventSynchronize(s->tev[4]));
+  float m1 = 0.f, m2 = 0.f;
+  SCUDA(cudaEventElapsedTime(&m1, s->tev[2], s->tev[3]));
+  SCUDA(cudaEventElapsedTime(&m2, s->tev[3], s->tev[4]));
+  *prec += m1;
+  *kry += m2;
+  return 0;
+}
+
 int device_be_solve(_p_TDy *t, double dt, double *dU, const TDyNewtonOptions &o, TDyNewtonStats *stats,
                     int *inst_its, double *inst_rel, void *stream) {
   int ierr;
@@ -1346,6 +1407,8 @@ int device_be_solve(_p_TDy *t, double dt, double *dU, const TDyNewtonOptions &o,
   long long lin_total = 0;
   int fell_back = 0;
   std::vector<int> trial_list;
+  double t_eval = 0.0, t_prec = 0.0, t_kry = 0.0;  // ms on the stream
+  int inner_redo = 0;  // FP32 inner solves redone in FP64 (instances x Newton iterations)
   // F and J at x (= xb for every instance after each evaluation below), and
   // the squared per-instance residual norms into g2
   // `sub` (host list of instances, or null for all): only those instances'
@@ -1386,15 +1449,20 @@ int device_be_solve(_p_TDy *t, double dt, double *dU, const TDyNewtonOptions &o,
     bool part = sub && (int)sub->size() < ns && device_inst_ok(t);
     if (part)  // one CTA per instance: only for instances small enough for one SM
       for (int g : *sub) part = part && s->h_seg_off[g + 1] - s->h_seg_off[g] <= 65536;
+    SCUDA(cudaEventRecord(s->tev[0], st));
     if (part)
       e = device_eval_instances(t, s->x, s->F, s->J, sub->data(), (int)sub->size(), st);
     else
       e = eval_all();
     if (e) return e;
+    SCUDA(cudaEventRecord(s->tev[1], st));
     seg_dot<double, double>(s, s->F, s->F, nullptr, nullptr, s->fn2, nullptr, st);
     SCUDA(cudaGetLastError());
     SCUDA(cudaMemcpyAsync(g2.data(), s->fn2, sizeof(double) * ns, cudaMemcpyDeviceToHost, st));
     SCUDA(cudaStreamSynchronize(st));
+    float ms = 0.f;
+    SCUDA(cudaEventElapsedTime(&ms, s->tev[0], s->tev[1]));
+    t_eval += ms;
     return 0;
   };
   if ((ierr = evaluate(masked ? &live : nullptr))) return ierr;
@@ -1427,10 +1495,40 @@ int device_be_solve(_p_TDy *t, double dt, double *dU, const TDyNewtonOptions &o,
     if (o.linear_fp32 && !fp32) fell_back = 1;
     const void *y;
     if (fp32) {
-      ierr = linear_solve<float>(s, s->k32, o, st, &lin_total, lin_its);
+      // FP32 inner solves stop after a quarter of linear_max_it (at least 20
+      // iterations); one that runs out (FP32 rounding can stall BiCGStab
+      // above the tolerance on ill-conditioned Jacobians) is solved again in
+      // FP64 with the full count, and the instance steps along that direction
+      // (kept in the FP32 array).  The choice depends on the instance alone,
+      // so it is the same alone and in a batch.
+      TDyNewtonOptions o32 = o;
+      o32.linear_max_it = std::min(o.linear_max_it, std::max(20, o.linear_max_it / 4));
+      ierr = linear_solve<float>(s, s->k32, o32, st, &lin_total, lin_its);
+      if (ierr) return ierr;
+      if ((ierr = add_linear_times(s, &t_prec, &t_kry))) return ierr;
+      std::vector<int> redo(ns, 0);
+      bool any_redo = false;
+      for (int g = 0; g < ns; g++)
+        if (act[g] && lin_its[g] >= o32.linear_max_it) any_redo = redo[g] = 1;
+      if (any_redo) {
+        SCUDA(cudaMemcpyAsync(s->newt_active, redo.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, st));
+        std::vector<int> lin64;
+        if ((ierr = linear_solve<double>(s, s->k64, o, st, &lin_total, lin64))) return ierr;
+        if ((ierr = add_linear_times(s, &t_prec, &t_kry))) return ierr;
+        cast_masked_kernel<<<nblk(n, 256), 256, 0, st>>>(n, s->cell_seg, s->newt_active, (const double *)s->k64.y,
+                                                         (float *)s->k32.y);
+        SCUDA(cudaMemcpyAsync(s->newt_active, act.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, st));
+        SCUDA(cudaStreamSynchronize(st));  // redo and act (host vectors) stay valid until here
+        for (int g = 0; g < ns; g++)
+          if (redo[g]) {
+            lin_its[g] = lin64[g];
+            inner_redo++;
+          }
+      }
       y = s->k32.y;
     } else {
       ierr = linear_solve<double>(s, s->k64, o, st, &lin_total, lin_its);
+      if (!ierr) ierr = add_linear_times(s, &t_prec, &t_kry);
       y = s->k64.y;
     }
     if (ierr) return ierr;
@@ -1567,6 +1665,10 @@ int device_be_solve(_p_TDy *t, double dt, double *dU, const TDyNewtonOptions &o,
     stats->cluster_cells_diagonal = s->precond_used == TDY_PRECOND_CLUSTERS ? s->ncl_big_cells : 0;
     stats->fp64_fallback = fell_back;
     stats->eval_schedule = s->eval_mode;
+    stats->eval_s = 1e-3 * t_eval;
+    stats->precond_s = 1e-3 * t_prec;
+    stats->krylov_s = 1e-3 * t_kry;
+    stats->fp64_inner_redo = inner_redo;
     stats->block_instances = s->precond_used == TDY_PRECOND_LINES ? s->n_block : 0;
     stats->block_max_cells = s->precond_used == TDY_PRECOND_LINES ? s->mask_for : -1;
   }

@@ -188,3 +188,36 @@ def test_oracle_threaded_residual_matches_serial():
     R, M = o.snes_function(U, with_mag=True)
     Rp = o.snes_function_parallel(U, 4)
     assert np.all(np.abs(Rp - R) <= 1e-13 * M)
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """The ctypes mirrors of the header's structs have the C compiler's sizes
+    and field offsets (a field added on one side only would shift the rest)."""
+    import ctypes
+    import shutil
+    import subprocess
+    from pathlib import Path
+
+    import tdycore_gb300 as T
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    root = Path(__file__).resolve().parent.parent
+    fields = {"TDyNewtonStats": T.NewtonStats, "TDyNewtonOptions": T.NewtonOptions}
+    lines = []
+    for cname, cls in fields.items():
+        lines.append(f'printf("%zu\\n", sizeof({cname}));')
+        for f, _ in cls._fields_:
+            lines.append(f'printf("%zu\\n", offsetof({cname}, {f}));')
+    src = tmp_path / "layout.c"
+    src.write_text("#include <stdio.h>\n#include <stddef.h>\n#include \"tdycore_gb300.h\"\nint main(void) {\n"
+                   + "\n".join(lines) + "\nreturn 0;\n}\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", str(root / "include"), "-o", str(exe), str(src)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    want = []
+    for cls in fields.values():
+        want.append(ctypes.sizeof(cls))
+        want += [getattr(cls, f).offset for f, _ in cls._fields_]
+    assert got == want

@@ -214,3 +214,29 @@ def test_tile_and_block_schedules_give_the_same_bits(fp32):
         assert np.array_equal(out[sched][1], out["tile"][1]), sched
         assert out[sched][2]["linear_iterations"] == out["tile"][2]["linear_iterations"], sched
     assert out["tile"][2]["converged"] + out["tile"][2]["step_converged"] == 24
+
+
+@pytest.mark.parametrize("fp32", [True, False])
+def test_spmv_threads_per_row_give_the_same_bits(fp32):
+    """The inner solve's sparse products sum each row in 8 phases added by a
+    fixed tree whatever the threads per row: 1, 2, 4 and 8 threads, on the
+    tile and the block schedule, give every instance the same bits and the
+    same iteration counts (so the timed choice, kept per process, never
+    changes a result)."""
+    import torch
+
+    T.options_clear()
+    tb, U0, info = batched_columns(24, seed_offset=9)
+    tb.setup()
+    ref = None
+    for sched in ("tile", "block"):
+        for tpr in (1, 2, 4, 8):
+            d = torch.tensor(U0, dtype=torch.float64, device="cuda")
+            st, its, rel = tb.backward_euler_step_device(d, DT, rtol=RTOL, fp32=fp32, schedule=sched,
+                                                         spmv_threads=tpr)
+            got = (d.cpu().numpy(), its.copy(), st["linear_iterations"])
+            if ref is None:
+                ref = got
+                continue
+            assert np.array_equal(got[0], ref[0]), (sched, tpr)
+            assert np.array_equal(got[1], ref[1]) and got[2] == ref[2], (sched, tpr)
