@@ -835,6 +835,41 @@ __device__ __forceinline__ void canon_vertex_pair(const DevArgs &a, int vc, int 
   }
 }
 
+// Entry (c, b) of another vertex's J_v in double-float: the rows r of
+// local cell c, in row order, each add -+w_r T_rb and, where b is the row's
+// up or down cell, -+E; every product at the entry's own power-of-two scale
+// (the largest exponent among its terms), as for the canonical vertices.
+// row_of(k), k < kn, lists the rows to scan; rows not touching c are skipped.
+template <class RowOf>
+__device__ __forceinline__ double gen_entry_ff(int c, int b, int kn, RowOf row_of, const int *lup, const int *ldn,
+                                               const double *w, const double *Eu, const double *Ed, const double *T,
+                                               int ncol) {
+  int mb = 0;
+  for (int k = 0; k < kn; k++) {
+    const int r = row_of(k), lu = lup[r], ld = ldn[r];
+    if (lu != c && ld != c) continue;
+    mb = max(mb, d_bexp(w[r]) + d_bexp(T[(size_t)r * ncol + b]) - 1023);
+    if (b == lu) mb = max(mb, d_bexp(Eu[r]));
+    if (b == ld) mb = max(mb, d_bexp(Ed[r]));
+  }
+  ff acc = {0.0f, 0.0f};
+  for (int k = 0; k < kn; k++) {
+    const int r = row_of(k), lu = lup[r], ld = ldn[r];
+    if (lu != c && ld != c) continue;
+    const bool isup = lu == c;
+    const double wr = w[r], t = T[(size_t)r * ncol + b];
+    const int bw = d_bexp(wr);
+    const ff p = ff_mul(ff_split_scaled(wr, bw, 1023 - bw), ff_split_scaled(t, d_bexp(t), bw - mb));
+    ff_acc(acc, isup ? ff_neg(p) : p);
+    if (b == lu || b == ld) {
+      const double et = b == lu ? Eu[r] : Ed[r];
+      const ff ef = ff_split_scaled(et, d_bexp(et), 1023 - mb);
+      ff_acc(acc, isup ? ff_neg(ef) : ef);
+    }
+  }
+  return ff_to_d(acc, mb - 1023);
+}
+
 // ---------------------------------------------------------------------------
 // 3. other vertices.  Both forms below sum every Jacobian entry (c, b) of a
 // vertex block over the rows whose faces touch local cell c in row order,
@@ -892,7 +927,12 @@ __device__ __forceinline__ void generic_vertex_one(const DevArgs &a, int g) {
       Rv[c] = s;
     }
   }
-  if (a.needJ) {
+  if (a.needJ && a.jac_ff) {
+    for (int c = 0; c < nint; c++)
+      for (int b = 0; b < nint; b++)
+        Jv[c * nint + b] = gen_entry_ff(c, b, nrow, [](int k) { return k; }, a.row_lup + r0, a.row_ldn + r0, w, Eu, Ed,
+                                        T, ncol);
+  } else if (a.needJ) {
     for (int c = 0; c < nint; c++) {
       for (int b = 0; b < nint; b++) Jv[c * nint + b] = 0.0;
       for (int r = 0; r < nrow; r++) {
@@ -992,6 +1032,16 @@ __device__ __forceinline__ void generic_vertex_warp(const DevArgs &a, int block)
   }
   if (!a.needJ) return;
   const int nn = nint * nint;
+  if (a.jac_ff) {
+    for (int e = lane; e < nn; e += 32) {
+      const int c = e / nint, b = e - c * nint;
+      const int kc = cnt[c];
+      const unsigned char *lc = lst + c * kGenCellRows;
+      Jv[e] = gen_entry_ff(c, b, kc == 255 ? nrow : kc, [&](int k) { return kc == 255 ? k : (int)lc[k]; }, lup, ldn,
+                           w, Eu, Ed, T, ncol);
+    }
+    return;
+  }
   for (int e = lane; e < nn; e += 32) {
     const int c = e / nint, b = e - c * nint;
     const int kc = cnt[c];
