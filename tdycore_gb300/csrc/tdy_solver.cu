@@ -877,13 +877,10 @@ int krylov_alloc(SolverState *s, Krylov &k, cudaStream_t st) {
   return 0;
 }
 
-// Picks the spmv threads per row by timing the candidates on the first solve
-// of the process and keeps the choice for every later handle (a server's
-// handles skip the timing); options.spmv_threads forces one.  The results do
-// not depend on it (row_dot).
-std::mutex g_tpr_mutex;
-int g_tpr[2] = {0, 0};  // float, double
-
+// Picks the spmv threads per row by timing the candidates on the handle's
+// first solve in each precision (the best split depends on the rows and on
+// the schedule); options.spmv_threads forces one.  The results do not depend
+// on it (row_dot).
 template <class T>
 int autotune_spmv(SolverState *s, Krylov &k, int forced, cudaStream_t st) {
   if (forced > 0) {
@@ -891,12 +888,6 @@ int autotune_spmv(SolverState *s, Krylov &k, int forced, cudaStream_t st) {
     return 0;
   }
   if (k.tpr) return 0;
-  std::lock_guard<std::mutex> lk(g_tpr_mutex);
-  int &cached = g_tpr[sizeof(T) == sizeof(double) ? 1 : 0];
-  if (cached) {
-    k.tpr = cached;
-    return 0;
-  }
   cudaEvent_t e0, e1;
   SCUDA(cudaEventCreate(&e0));
   SCUDA(cudaEventCreate(&e1));
@@ -918,7 +909,6 @@ int autotune_spmv(SolverState *s, Krylov &k, int forced, cudaStream_t st) {
     }
   }
   k.tpr = best_tpr;
-  cached = best_tpr;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   return 0;
