@@ -221,3 +221,16 @@ def test_struct_layouts_match_the_header(tmp_path):
         want.append(ctypes.sizeof(cls))
         want += [getattr(cls, f).offset for f, _ in cls._fields_]
     assert got == want
+
+
+def test_newton_option_defaults():
+    """TDyNewtonOptionsDefault (no device needed) sets PETSc's SNES defaults
+    and the mixed-precision defaults the documentation states."""
+    import ctypes
+
+    o = T.NewtonOptions()
+    assert T.lib.TDyNewtonOptionsDefault(ctypes.byref(o)) == 0
+    assert (o.rtol, o.atol, o.max_it, o.stol) == (1e-8, 0.0, 50, 1e-8)
+    assert (o.linear_fp32, o.linear_rtol, o.linear_max_it) == (1, 1e-6, 400)
+    assert (o.precond, o.cluster_threshold) == (T.PRECOND_LINES, 0.05)
+    assert (o.schedule, o.fp32_max_it, o.spmv_threads) == (T.SCHEDULE_AUTO, 8, 0)
