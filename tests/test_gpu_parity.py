@@ -1,6 +1,6 @@
 """GPU residual/Jacobian parity with the oracle (C restatement of the reference).
 
-Tolerances (stated per the spec bar, FP64):
+Tolerances (FP64):
   residual:  |R_gpu - R_ref| <= 1e-12 * sum_k |terms_k into cell i|  (per cell)
   Jacobian:  |J_gpu - J_ref| <= 1e-10 * sum_k |contributions_k|      (per entry)
 The right-hand sides are the floating-point error scale of each summed
