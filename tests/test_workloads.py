@@ -43,3 +43,33 @@ def test_random_spd_rotations_and_anisotropy():
     ev = np.log10(np.linalg.eigvalsh(K))
     assert abs(ev.mean() + 12.0) < 0.05 and abs(ev.std() - 1.0) < 0.05
     assert np.std(ev[:, 2] - ev[:, 0]) < 1.0
+
+
+def test_workloads_are_seeded():
+    """Every generator the bench uses is seeded: two builds give the same
+    mesh, materials, boundary data and start, so both arms and every run see
+    the same inputs."""
+    import tdycore_gb300 as T
+    from tdycore_gb300 import workloads as W
+
+    def view(build):
+        T.options_clear()
+        t, U = build()
+        t.setup(host_only=True)
+        v = t.setup_view()
+        t.destroy()
+        return v, U
+
+    builds = {
+        "spe10_like": lambda: W.spe10_like(8, 7, 5, seed_offset=3)[:2],
+        "batched_columns": lambda: W.batched_columns(12)[:2],
+        "infiltration_prisms": lambda: W.infiltration_prisms(60, 4)[:2],
+    }
+    for name, build in builds.items():
+        (v1, U1), (v2, U2) = view(build), view(build)
+        assert np.array_equal(U1, U2), name
+        for k, a in v1.items():
+            if isinstance(a, np.ndarray):
+                assert np.array_equal(a, v2[k]), (name, k)
+            else:
+                assert a == v2[k], (name, k)
